@@ -1,0 +1,583 @@
+// Host side of the C ABI (include/cwgpu.h): context, device layout, pair
+// ordering, persistent graph-captured launch, plain one-launch-per-pair form.
+//
+// Device layout in HBM (all resident for the life of the context):
+//   codes   int8 residues, every sequence starting at a 16-byte boundary
+//   offs    int64 start of each sequence in `codes`
+//   lens    int32 sequence lengths n (getSeqLength)
+//   nres    int32 residues that are not gapPos1/gapPos2 (len1/len2 of :100-127)
+//   go_tab  int32 gap-open penalty per min(n, m) (FullPairwiseAlign.cpp:129-146)
+//   matrix  int32[32*32] pairwise substitution matrix
+//   scratch int2[slots][2][lmax+1]: per warp slot, the boundary rows of the
+//           forward and reverse sweeps (HH/DD and RR/SS of diff()).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "cwgpu.h"
+#include "cwgpu_device.cuh"
+
+namespace {
+
+constexpr int kR = 4;             // rows per lane in the wavefront sweeps
+constexpr int kWarpsPerBlock = 4; // warps (= concurrent pairs) per CTA
+constexpr size_t kProfBytesPerWarp = 32 * 32 * kR * sizeof(uint16_t);
+
+__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+    k_pairwise(cwgpu::PairArgs g, long long single) {
+    __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
+    extern __shared__ __align__(16) uint16_t prof_all[];
+    for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = g.matrix[i];
+    __syncthreads();
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int wpb = blockDim.x >> 5;
+    const long long slot = (long long)blockIdx.x * wpb + warp;
+    uint16_t* prof = prof_all + (size_t)warp * (kProfBytesPerWarp / sizeof(uint16_t));
+    int2* bufA = g.scratch + (size_t)slot * 2 * (g.lmax + 1);
+    int2* bufB = bufA + (g.lmax + 1);
+    if (single >= 0) {
+        if (slot == 0) cwgpu::align_pair<kR>(g, single, prof, smat, bufA, bufB);
+        return;
+    }
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(g.counter, 1ULL);
+        k = __shfl_sync(cwgpu::kFull, k, 0);
+        if (k >= (unsigned long long)g.npairs) break;
+        cwgpu::align_pair<kR>(g, (long long)g.order[k], prof, smat, bufA, bufB);
+    }
+}
+
+}  // namespace
+
+struct cwgpu_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    bool has_matrix = false, has_params = false, has_seqs = false;
+    int32_t matrix[CWGPU_NUMRES * CWGPU_NUMRES];
+    cwgpu_params params;
+    int nseqs = 0;
+    int lmax = 0;
+    std::vector<int32_t> lens;
+    std::vector<int64_t> offs;
+    std::vector<int8_t> host_codes;  // for nres recomputation when params change
+    int8_t* d_codes = nullptr;
+    int64_t* d_offs = nullptr;
+    int32_t* d_lens = nullptr;
+    int32_t* d_nres = nullptr;
+    int32_t* d_matrix = nullptr;
+    int32_t* d_go = nullptr;
+    int go_len = 0;
+    int2* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    unsigned long long* d_counter = nullptr;
+    int* d_err = nullptr;
+    int grid = 0;
+    bool derived_dirty = true;
+    unsigned generation = 0;  // bumped whenever device inputs or scratch move
+    std::string last_error;
+};
+
+struct cwgpu_plan {
+    cwgpu_context* ctx = nullptr;
+    int64_t npairs = 0;
+    int32_t* d_pairs = nullptr;
+    int32_t* d_order = nullptr;
+    float* d_dist = nullptr;
+    cwgpu_pair_stats* d_stats = nullptr;
+    cudaGraph_t graph = nullptr;
+    cudaGraphExec_t exec = nullptr;
+    cudaStream_t graph_stream = nullptr;
+    unsigned generation = 0;
+};
+
+namespace {
+
+int fail(cwgpu_context* ctx, int code, const std::string& msg) {
+    if (ctx) ctx->last_error = msg;
+    return code;
+}
+
+int cuda_fail(cwgpu_context* ctx, cudaError_t e, const char* what) {
+    std::string m = std::string(what) + ": " + cudaGetErrorString(e);
+    return fail(ctx, e == cudaErrorMemoryAllocation ? CWGPU_ERR_OOM : CWGPU_ERR_CUDA, m);
+}
+
+#define CW_CUDA(ctx, call)                                      \
+    do {                                                        \
+        cudaError_t e_ = (call);                                \
+        if (e_ != cudaSuccess) return cuda_fail(ctx, e_, #call); \
+    } while (0)
+
+template <class T>
+void dfree(T*& p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+// Recomputes nres and the gap-open table after sequences or params changed.
+int refresh_derived(cwgpu_context* ctx) {
+    if (!ctx->derived_dirty) return CWGPU_OK;
+    if (!ctx->has_params || !ctx->has_seqs) return fail(ctx, CWGPU_ERR_STATE, "params or sequences not set");
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    std::vector<int32_t> nres(ctx->nseqs);
+    for (int s = 0; s < ctx->nseqs; ++s) {
+        int c = 0;
+        const int8_t* p = ctx->host_codes.data() + ctx->offs[s];
+        for (int i = 0; i < ctx->lens[s]; ++i)
+            if (p[i] != ctx->params.gap_pos1 && p[i] != ctx->params.gap_pos2) ++c;
+        nres[s] = c;
+    }
+    dfree(ctx->d_nres);
+    CW_CUDA(ctx, cudaMalloc(&ctx->d_nres, sizeof(int32_t) * std::max(1, ctx->nseqs)));
+    if (ctx->nseqs)
+        CW_CUDA(ctx, cudaMemcpy(ctx->d_nres, nres.data(), sizeof(int32_t) * ctx->nseqs, cudaMemcpyHostToDevice));
+    std::vector<int32_t> go(ctx->lmax + 1);
+    for (int L = 1; L <= ctx->lmax; ++L) {  // L = 0 pairs never reach the penalties (:113-118)
+        int32_t g = 0, e = 0;
+        cwgpu_gap_penalties(&ctx->params, L, L, &g, &e);
+        go[L] = g;
+    }
+    dfree(ctx->d_go);
+    CW_CUDA(ctx, cudaMalloc(&ctx->d_go, sizeof(int32_t) * go.size()));
+    CW_CUDA(ctx, cudaMemcpy(ctx->d_go, go.data(), sizeof(int32_t) * go.size(), cudaMemcpyHostToDevice));
+    ctx->go_len = (int)go.size();
+    ctx->derived_dirty = false;
+    ctx->generation++;
+    return CWGPU_OK;
+}
+
+int gap_extend_of(const cwgpu_params& p) {
+    int32_t g = 0, e = 0;
+    cwgpu_gap_penalties(&p, 1, 1, &g, &e);
+    return e;
+}
+
+// Persistent grid: as many CTAs as fit on every SM at once.
+int ensure_scratch(cwgpu_context* ctx) {
+    if (ctx->grid == 0) {
+        int per_sm = 0;
+        const size_t smem = kProfBytesPerWarp * kWarpsPerBlock;
+        CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        CW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise, kWarpsPerBlock * 32, smem));
+        if (per_sm < 1) per_sm = 1;
+        ctx->grid = per_sm * ctx->sm_count;
+    }
+    const size_t need = (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1) * sizeof(int2);
+    if (need > ctx->scratch_bytes) {
+        dfree(ctx->d_scratch);
+        ctx->scratch_bytes = 0;
+        CW_CUDA(ctx, cudaMalloc(&ctx->d_scratch, need));
+        ctx->scratch_bytes = need;
+        ctx->generation++;
+    }
+    return CWGPU_OK;
+}
+
+cwgpu::PairArgs make_args(cwgpu_context* ctx, const int32_t* d_pairs, const int32_t* d_order, int64_t npairs,
+                          float* d_dist, cwgpu_pair_stats* d_stats) {
+    cwgpu::PairArgs g;
+    g.codes = ctx->d_codes;
+    g.offs = ctx->d_offs;
+    g.lens = ctx->d_lens;
+    g.nres = ctx->d_nres;
+    g.pairs = d_pairs;
+    g.order = d_order;
+    g.go_table = ctx->d_go;
+    g.matrix = ctx->d_matrix;
+    g.dist = d_dist;
+    g.stats = d_stats;
+    g.scratch = ctx->d_scratch;
+    g.counter = ctx->d_counter;
+    g.err = ctx->d_err;
+    g.npairs = npairs;
+    g.lmax = ctx->lmax;
+    g.ge = gap_extend_of(ctx->params);
+    g.gp1 = ctx->params.gap_pos1;
+    g.gp2 = ctx->params.gap_pos2;
+    return g;
+}
+
+int check_ready(cwgpu_context* ctx) {
+    if (!ctx) return CWGPU_ERR_ARG;
+    if (!ctx->has_matrix) return fail(ctx, CWGPU_ERR_STATE, "matrix not set");
+    if (!ctx->has_params) return fail(ctx, CWGPU_ERR_STATE, "params not set");
+    if (!ctx->has_seqs) return fail(ctx, CWGPU_ERR_STATE, "sequences not uploaded");
+    int rc = refresh_derived(ctx);
+    if (rc) return rc;
+    return ensure_scratch(ctx);
+}
+
+int validate_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs) {
+    if (npairs < 0 || (npairs > 0 && !pairs)) return fail(ctx, CWGPU_ERR_ARG, "bad pair list");
+    for (int64_t q = 0; q < npairs; ++q) {
+        const int32_t a = pairs[2 * q], b = pairs[2 * q + 1];
+        if (a < 0 || a >= ctx->nseqs || b < 0 || b >= ctx->nseqs)
+            return fail(ctx, CWGPU_ERR_ARG, "pair index out of range");
+    }
+    return CWGPU_OK;
+}
+
+// Longest pairs first, so the tail of the persistent queue holds short work.
+std::vector<int32_t> work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs) {
+    std::vector<int32_t> order((size_t)npairs);
+    std::iota(order.begin(), order.end(), 0);
+    std::vector<int64_t> work((size_t)npairs);
+    for (int64_t q = 0; q < npairs; ++q)
+        work[q] = (int64_t)ctx->lens[pairs[2 * q]] * (int64_t)ctx->lens[pairs[2 * q + 1]];
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work[x] > work[y]; });
+    return order;
+}
+
+int check_kernel_error(cwgpu_context* ctx) {
+    int err = 0;
+    CW_CUDA(ctx, cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) {
+        CW_CUDA(ctx, cudaMemset(ctx->d_err, 0, sizeof(int)));
+        return fail(ctx, CWGPU_ERR_DEVICE, "kernel reported an internal limit (Myers-Miller stack depth)");
+    }
+    return CWGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* cwgpu_status_string(int status) {
+    switch (status) {
+        case CWGPU_OK: return "ok";
+        case CWGPU_ERR_ARG: return "invalid argument";
+        case CWGPU_ERR_CUDA: return "CUDA error";
+        case CWGPU_ERR_OOM: return "out of device memory";
+        case CWGPU_ERR_STATE: return "inputs not set";
+        case CWGPU_ERR_RANGE: return "the range for pairwise alignment is incorrect";
+        case CWGPU_ERR_TIMEOUT: return "bounded device wait timed out";
+        case CWGPU_ERR_DEVICE: return "device-side limit exceeded";
+        case CWGPU_ERR_MATRIX: return "matrix entry outside int16";
+        case CWGPU_ERR_NOT_FOUND: return "unknown job";
+        default: return "unknown status";
+    }
+}
+
+const char* cwgpu_last_error(const cwgpu_context* ctx) { return ctx ? ctx->last_error.c_str() : ""; }
+
+int cwgpu_gap_penalties(const cwgpu_params* p, int32_t n, int32_t m, int32_t* gap_open, int32_t* gap_extend) {
+    if (!p || !gap_open || !gap_extend) return CWGPU_ERR_ARG;
+    // FullPairwiseAlign.cpp:129-148 with the reference's operand types: float
+    // members times int intScale stay float; the protein gap-open goes through
+    // double because log() returns double.
+    if (p->dna) {
+        *gap_open = static_cast<int>(2 * p->pw_gap_open * p->int_scale * p->gap_open_scale);
+        *gap_extend = static_cast<int>(p->pw_gap_extend * p->int_scale * p->gap_extend_scale);
+    } else {
+        const int mn = n < m ? n : m;
+        if (p->mat_avg <= 0)
+            *gap_open = 2 * static_cast<int>((p->pw_gap_open + log(static_cast<double>(mn))) * p->int_scale);
+        else
+            *gap_open = static_cast<int>(2 * p->mat_avg * (p->pw_gap_open + log(static_cast<double>(mn))) *
+                                         p->gap_open_scale);
+        *gap_extend = static_cast<int>(p->pw_gap_extend * p->int_scale);
+    }
+    return CWGPU_OK;
+}
+
+int64_t cwgpu_range_pair_count(int32_t nseqs, int32_t i_start, int32_t i_end, int32_t j_start, int32_t j_end) {
+    int64_t c = 0;
+    for (int32_t si = std::max(0, i_start); si < nseqs && si < i_end; ++si) {
+        const int32_t lo = std::max(si + 1, j_start + 1);
+        const int32_t hi = std::min(nseqs, j_end);
+        if (hi > lo) c += hi - lo;
+    }
+    return c;
+}
+
+int cwgpu_create(int device, cwgpu_context** out) {
+    if (!out) return CWGPU_ERR_ARG;
+    *out = nullptr;
+    cwgpu_context* ctx = new (std::nothrow) cwgpu_context();
+    if (!ctx) return CWGPU_ERR_OOM;
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_matrix, sizeof(int32_t) * CWGPU_NUMRES * CWGPU_NUMRES);
+    if (e != cudaSuccess) {
+        cwgpu_destroy(ctx);
+        return e == cudaErrorMemoryAllocation ? CWGPU_ERR_OOM : CWGPU_ERR_CUDA;
+    }
+    memset(&ctx->params, 0, sizeof(ctx->params));
+    *out = ctx;
+    return CWGPU_OK;
+}
+
+void cwgpu_destroy(cwgpu_context* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    dfree(ctx->d_codes);
+    dfree(ctx->d_offs);
+    dfree(ctx->d_lens);
+    dfree(ctx->d_nres);
+    dfree(ctx->d_matrix);
+    dfree(ctx->d_go);
+    dfree(ctx->d_scratch);
+    dfree(ctx->d_counter);
+    dfree(ctx->d_err);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+int cwgpu_set_matrix(cwgpu_context* ctx, const int32_t* matrix) {
+    if (!ctx || !matrix) return CWGPU_ERR_ARG;
+    for (int i = 0; i < CWGPU_NUMRES * CWGPU_NUMRES; ++i)
+        if (matrix[i] < -32768 || matrix[i] > 32767)
+            return fail(ctx, CWGPU_ERR_MATRIX, "matrix entry outside the int16 profile range");
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    memcpy(ctx->matrix, matrix, sizeof(ctx->matrix));
+    CW_CUDA(ctx, cudaMemcpy(ctx->d_matrix, matrix, sizeof(ctx->matrix), cudaMemcpyHostToDevice));
+    ctx->has_matrix = true;
+    ctx->generation++;
+    return CWGPU_OK;
+}
+
+int cwgpu_set_params(cwgpu_context* ctx, const cwgpu_params* params) {
+    if (!ctx || !params) return CWGPU_ERR_ARG;
+    ctx->params = *params;
+    ctx->has_params = true;
+    ctx->derived_dirty = true;
+    ctx->generation++;
+    return CWGPU_OK;
+}
+
+int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, const int64_t* offsets,
+                      const int32_t* lens) {
+    if (!ctx || nseqs < 0 || (nseqs > 0 && (!offsets || !lens))) return CWGPU_ERR_ARG;
+    std::vector<int64_t> doffs(nseqs);
+    int64_t total = 0;
+    int lmax = 0;
+    for (int s = 0; s < nseqs; ++s) {
+        if (lens[s] < 0 || lens[s] > CWGPU_MAX_SEQ_LEN)
+            return fail(ctx, CWGPU_ERR_ARG, "sequence length outside [0, CWGPU_MAX_SEQ_LEN]");
+        if (lens[s] > 0 && (!codes || offsets[s] < 0)) return fail(ctx, CWGPU_ERR_ARG, "bad sequence offset");
+        for (int i = 0; i < lens[s]; ++i) {
+            const int8_t c = codes[offsets[s] + i];
+            if (c < 0 || c >= CWGPU_NUMRES) return fail(ctx, CWGPU_ERR_ARG, "residue code outside [0, 31]");
+        }
+        doffs[s] = total;
+        total += (lens[s] + 15) & ~15;
+        lmax = std::max(lmax, (int)lens[s]);
+    }
+    std::vector<int8_t> packed((size_t)std::max<int64_t>(total, 16), 0);
+    for (int s = 0; s < nseqs; ++s)
+        if (lens[s] > 0) memcpy(packed.data() + doffs[s], codes + offsets[s], lens[s]);
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    dfree(ctx->d_codes);
+    dfree(ctx->d_offs);
+    dfree(ctx->d_lens);
+    ctx->has_seqs = false;
+    CW_CUDA(ctx, cudaMalloc(&ctx->d_codes, packed.size()));
+    CW_CUDA(ctx, cudaMalloc(&ctx->d_offs, sizeof(int64_t) * std::max(1, nseqs)));
+    CW_CUDA(ctx, cudaMalloc(&ctx->d_lens, sizeof(int32_t) * std::max(1, nseqs)));
+    CW_CUDA(ctx, cudaMemcpy(ctx->d_codes, packed.data(), packed.size(), cudaMemcpyHostToDevice));
+    if (nseqs) {
+        CW_CUDA(ctx, cudaMemcpy(ctx->d_offs, doffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
+        CW_CUDA(ctx, cudaMemcpy(ctx->d_lens, lens, sizeof(int32_t) * nseqs, cudaMemcpyHostToDevice));
+    }
+    ctx->nseqs = nseqs;
+    ctx->lmax = lmax;
+    ctx->lens.assign(lens, lens + nseqs);
+    ctx->offs = doffs;
+    ctx->host_codes.swap(packed);
+    ctx->has_seqs = true;
+    ctx->derived_dirty = true;
+    ctx->generation++;
+    return CWGPU_OK;
+}
+
+// ---- plans: device-resident pair list + captured launch -------------------
+
+int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, cwgpu_plan** out) {
+    if (!ctx || !out) return CWGPU_ERR_ARG;
+    *out = nullptr;
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    rc = validate_pairs(ctx, pairs, npairs);
+    if (rc) return rc;
+    cwgpu_plan* p = new (std::nothrow) cwgpu_plan();
+    if (!p) return CWGPU_ERR_OOM;
+    p->ctx = ctx;
+    p->npairs = npairs;
+    const size_t np = (size_t)std::max<int64_t>(npairs, 1);
+    cudaError_t e = cudaMalloc(&p->d_pairs, sizeof(int32_t) * 2 * np);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_order, sizeof(int32_t) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_dist, sizeof(float) * np);
+    if (e == cudaSuccess) e = cudaMalloc(&p->d_stats, sizeof(cwgpu_pair_stats) * np);
+    if (e == cudaSuccess && npairs > 0) {
+        std::vector<int32_t> order = work_order(ctx, pairs, npairs);
+        e = cudaMemcpy(p->d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice);
+        if (e == cudaSuccess) e = cudaMemcpy(p->d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice);
+    }
+    if (e == cudaSuccess) {
+        // Capture: reset the queue counter, then one persistent launch.
+        cwgpu::PairArgs g = make_args(ctx, p->d_pairs, p->d_order, npairs, p->d_dist, p->d_stats);
+        const size_t smem = kProfBytesPerWarp * kWarpsPerBlock;
+        e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal);
+        if (e == cudaSuccess) {
+            cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), p->graph_stream);
+            if (npairs > 0) {
+                const int grid = (int)std::min<int64_t>(ctx->grid, (npairs + kWarpsPerBlock - 1) / kWarpsPerBlock);
+                k_pairwise<<<grid, kWarpsPerBlock * 32, smem, p->graph_stream>>>(g, -1);
+            }
+            e = cudaStreamEndCapture(p->graph_stream, &p->graph);
+        }
+        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+    }
+    if (e != cudaSuccess) {
+        cwgpu_plan_destroy(p);
+        return cuda_fail(ctx, e, "cwgpu_plan_create");
+    }
+    p->generation = ctx->generation;
+    *out = p;
+    return CWGPU_OK;
+}
+
+int cwgpu_plan_launch(cwgpu_plan* p, void* stream) {
+    if (!p) return CWGPU_ERR_ARG;
+    cwgpu_context* ctx = p->ctx;
+    if (p->generation != ctx->generation || ctx->derived_dirty)
+        return fail(ctx, CWGPU_ERR_STATE, "plan is stale: inputs changed after cwgpu_plan_create");
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+    CW_CUDA(ctx, cudaGraphLaunch(p->exec, s));
+    return CWGPU_OK;
+}
+
+int cwgpu_plan_results(cwgpu_plan* p, float* dist_out, cwgpu_pair_stats* stats_out) {
+    if (!p) return CWGPU_ERR_ARG;
+    cwgpu_context* ctx = p->ctx;
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    CW_CUDA(ctx, cudaDeviceSynchronize());
+    int rc = check_kernel_error(ctx);
+    if (rc) return rc;
+    if (p->npairs > 0 && dist_out)
+        CW_CUDA(ctx, cudaMemcpy(dist_out, p->d_dist, sizeof(float) * p->npairs, cudaMemcpyDeviceToHost));
+    if (p->npairs > 0 && stats_out)
+        CW_CUDA(ctx, cudaMemcpy(stats_out, p->d_stats, sizeof(cwgpu_pair_stats) * p->npairs, cudaMemcpyDeviceToHost));
+    return CWGPU_OK;
+}
+
+void* cwgpu_plan_device_dist(cwgpu_plan* p) { return p ? (void*)p->d_dist : nullptr; }
+
+void cwgpu_plan_destroy(cwgpu_plan* p) {
+    if (!p) return;
+    if (p->ctx) cudaSetDevice(p->ctx->device);
+    if (p->graph_stream) cudaStreamSynchronize(p->graph_stream);
+    if (p->exec) cudaGraphExecDestroy(p->exec);
+    if (p->graph) cudaGraphDestroy(p->graph);
+    if (p->graph_stream) cudaStreamDestroy(p->graph_stream);
+    dfree(p->d_pairs);
+    dfree(p->d_order);
+    dfree(p->d_dist);
+    dfree(p->d_stats);
+    delete p;
+}
+
+int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,
+                      cwgpu_pair_stats* stats_out) {
+    if (!ctx || (npairs > 0 && !dist_out)) return CWGPU_ERR_ARG;
+    cwgpu_plan* p = nullptr;
+    int rc = cwgpu_plan_create(ctx, pairs, npairs, &p);
+    if (rc) return rc;
+    rc = cwgpu_plan_launch(p, nullptr);
+    if (!rc) rc = cwgpu_plan_results(p, dist_out, stats_out);
+    cwgpu_plan_destroy(p);
+    return rc;
+}
+
+int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,
+                            cwgpu_pair_stats* stats_out) {
+    if (!ctx || (npairs > 0 && !dist_out)) return CWGPU_ERR_ARG;
+    int rc = check_ready(ctx);
+    if (rc) return rc;
+    rc = validate_pairs(ctx, pairs, npairs);
+    if (rc) return rc;
+    if (npairs == 0) return CWGPU_OK;
+    int32_t* d_pairs = nullptr;
+    float* d_dist = nullptr;
+    cwgpu_pair_stats* d_stats = nullptr;
+    cudaError_t e = cudaMalloc(&d_pairs, sizeof(int32_t) * 2 * npairs);
+    if (e == cudaSuccess) e = cudaMalloc(&d_dist, sizeof(float) * npairs);
+    if (e == cudaSuccess) e = cudaMalloc(&d_stats, sizeof(cwgpu_pair_stats) * npairs);
+    if (e == cudaSuccess) e = cudaMemcpy(d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        cwgpu::PairArgs g = make_args(ctx, d_pairs, nullptr, npairs, d_dist, d_stats);
+        for (int64_t q = 0; q < npairs && e == cudaSuccess; ++q) {
+            k_pairwise<<<1, 32, kProfBytesPerWarp, ctx->stream>>>(g, (long long)q);
+            e = cudaGetLastError();
+        }
+    }
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e == cudaSuccess) {
+        rc = check_kernel_error(ctx);
+        if (!rc) {
+            e = cudaMemcpy(dist_out, d_dist, sizeof(float) * npairs, cudaMemcpyDeviceToHost);
+            if (e == cudaSuccess && stats_out)
+                e = cudaMemcpy(stats_out, d_stats, sizeof(cwgpu_pair_stats) * npairs, cudaMemcpyDeviceToHost);
+        }
+    }
+    dfree(d_pairs);
+    dfree(d_dist);
+    dfree(d_stats);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cwgpu_align_pairs_plain");
+    return rc;
+}
+
+int cwgpu_pairwise_align(cwgpu_context* ctx, int32_t i_start, int32_t i_end, int32_t j_start, int32_t j_end,
+                         double* elements, int32_t dist_size, cwgpu_pair_stats* stats_out) {
+    if (!ctx || !elements) return CWGPU_ERR_ARG;
+    if (!ctx->has_seqs) return fail(ctx, CWGPU_ERR_STATE, "sequences not uploaded");
+    // FullPairwiseAlign.cpp:47-52
+    if (dist_size != ctx->nseqs + 1) return fail(ctx, CWGPU_ERR_ARG, "The distance matrix is not the right size!");
+    // FullPairwiseAlign.cpp:53-58
+    if (i_start < 0 || i_end < i_start || j_start < 0 || j_end < j_start)
+        return fail(ctx, CWGPU_ERR_RANGE, "The range for pairwise Alignment is incorrect.");
+    const int n = ctx->nseqs;
+    if (n == 0) return CWGPU_OK;  // :63-66
+    std::vector<int32_t> pairs;
+    for (int32_t si = std::max(0, i_start); si < n && si < i_end; ++si)
+        for (int32_t sj = std::max(si + 1, j_start + 1); sj < n && sj < j_end; ++sj) {
+            pairs.push_back(si);
+            pairs.push_back(sj);
+        }
+    const int64_t np = (int64_t)pairs.size() / 2;
+    std::vector<float> dist((size_t)std::max<int64_t>(np, 1));
+    int rc = cwgpu_align_pairs(ctx, pairs.data(), np, dist.data(), stats_out);
+    if (rc) return rc;
+    for (int64_t q = 0; q < np; ++q) {
+        // SymMatrix::getIndex for (si+1, sj+1), si < sj: ((_j*(_j+1))>>1) + _i.
+        const int64_t i = pairs[2 * q], j = pairs[2 * q + 1];
+        elements[((j * (j + 1)) >> 1) + i] = (double)dist[q];
+    }
+    return CWGPU_OK;
+}
+
+int cwgpu_synchronize(cwgpu_context* ctx) {
+    if (!ctx) return CWGPU_ERR_ARG;
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    CW_CUDA(ctx, cudaDeviceSynchronize());
+    return check_kernel_error(ctx);
+}
+
+}  // extern "C"

@@ -1,0 +1,167 @@
+/*
+ * cwgpu.h - C ABI of the GB300 (sm_103a) full-pairwise distance stage.
+ *
+ * This library computes what ClustalW 2.0.11's
+ * clustalw::FullPairwiseAlign::pairwiseAlign computes
+ * (CPU/clustalw-2.0.11/src/pairwise/FullPairwiseAlign.cpp:34-211): for every
+ * sequence pair, Gotoh local forward and reverse score sweeps, Myers-Miller
+ * linear-space alignment of the local segment, the identity count along that
+ * path and the distance (100 - 100*ident/min(len1,len2))/100 in float. Results
+ * are bit-identical to the reference on the same inputs.
+ *
+ * The reference plugin interface this replaces is the pure virtual
+ *   PairwiseAlignBase::pairwiseAlign(Alignment*, DistMatrix*, int iStart,
+ *                                    int iEnd, int jStart, int jEnd)
+ * (CPU/clustalw-2.0.11/src/pairwise/PairwiseAlignBase.h:19-20). The C++ class
+ * in cuda-clustalw_gb300/host/GpuFullPairwiseAlign.h implements it on top of
+ * these functions.
+ *
+ * Conventions: plain pointers and sizes only; sequence indices are 0-based
+ * (si, sj) like the reference's loop variables, and DistMatrix positions are
+ * the reference's 1-based (si+1, sj+1). Every call returns a cwgpu_status; no
+ * call exits the process. A context owns one CUDA device and is not
+ * thread-safe (like the reference class, which keeps static locals in diff()).
+ */
+#ifndef CWGPU_H
+#define CWGPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define CWGPU_NUMRES 32       /* clustalw NUMRES (general/clustalw.h:231) */
+#define CWGPU_MAX_SEQ_LEN 65535 /* longest sequence a context accepts */
+
+typedef enum cwgpu_status {
+    CWGPU_OK = 0,
+    CWGPU_ERR_ARG = 1,        /* bad pointer, size, code or range */
+    CWGPU_ERR_CUDA = 2,       /* a CUDA runtime call failed (see cwgpu_last_error) */
+    CWGPU_ERR_OOM = 3,        /* device allocation failed or over the memory budget */
+    CWGPU_ERR_STATE = 4,      /* matrix / params / sequences not set yet */
+    CWGPU_ERR_RANGE = 5,      /* iStart..jEnd range rejected (FullPairwiseAlign.cpp:53-58) */
+    CWGPU_ERR_TIMEOUT = 6,    /* a bounded device wait ran out */
+    CWGPU_ERR_DEVICE = 7,     /* the kernel reported an internal limit (stack depth) */
+    CWGPU_ERR_MATRIX = 8,     /* a matrix entry does not fit the int16 score profile */
+    CWGPU_ERR_NOT_FOUND = 9   /* unknown job id */
+} cwgpu_status;
+
+/* The scalars FullPairwiseAlign::pairwiseAlign reads from userParameters and
+ * from SubMatrix::getPairwiseMatrix (FullPairwiseAlign.cpp:69-94). */
+typedef struct cwgpu_params {
+    int32_t dna;            /* userParameters->getDNAFlag() */
+    float pw_gap_open;      /* userParameters->getPWGapOpen() */
+    float pw_gap_extend;    /* userParameters->getPWGapExtend() */
+    int32_t int_scale;      /* PairScaleValues::intScale */
+    float gap_open_scale;   /* PairScaleValues::gapOpenScale */
+    float gap_extend_scale; /* PairScaleValues::gapExtendScale */
+    int32_t mat_avg;        /* matAvg returned by getPairwiseMatrix */
+    int32_t gap_pos1;       /* userParameters->getGapPos1() */
+    int32_t gap_pos2;       /* userParameters->getGapPos2() */
+} cwgpu_params;
+
+/* Per-pair intermediate results (members of FullPairwiseAlign after the pair). */
+typedef struct cwgpu_pair_stats {
+    int32_t fwd_score; /* forwardPass maxScore (FullPairwiseAlign.cpp:285-338) */
+    int32_t se1, se2;  /* forwardPass end cell */
+    int32_t sb1, sb2;  /* reversePass start cell (:350-408) */
+    int32_t mm_score;  /* diff() return value (:165) */
+    int32_t n_ident;   /* tracePath identity count (:231-278) */
+    int32_t n_match;   /* aligned residue pairs on the Myers-Miller path */
+} cwgpu_pair_stats;
+
+typedef struct cwgpu_context cwgpu_context;
+
+/* ---- context ------------------------------------------------------------ */
+
+/* Creates a context on CUDA device `device`. No reference counterpart: the
+ * reference class allocates its scratch in pairwiseAlign (:74-78). */
+int cwgpu_create(int device, cwgpu_context** out);
+/* Frees all device memory of the context. Replaces ~FullPairwiseAlign. */
+void cwgpu_destroy(cwgpu_context* ctx);
+/* Static text for a status code. */
+const char* cwgpu_status_string(int status);
+/* Detail text of the last failure on this context ("" if none). */
+const char* cwgpu_last_error(const cwgpu_context* ctx);
+
+/* ---- inputs ------------------------------------------------------------- */
+
+/* The 32x32 int matrix from SubMatrix::getPairwiseMatrix
+ * (substitutionMatrix/SubMatrix.cpp:256-390), row-major matrix[a*32+b].
+ * Replaces the `matrix` member filled at FullPairwiseAlign.cpp:81. Entries
+ * must lie in [-32768, 32767]. */
+int cwgpu_set_matrix(cwgpu_context* ctx, const int32_t* matrix);
+/* Scalars of FullPairwiseAlign.cpp:69-94. */
+int cwgpu_set_params(cwgpu_context* ctx, const cwgpu_params* params);
+/* Uploads `nseqs` encoded sequences (SeqArray rows 1..nseqs without the dummy
+ * element 0, Alignment.h:96): sequence s is codes[offsets[s] .. offsets[s] +
+ * lens[s]), every code in [0, 31]. Replaces the getSeqArray()/getSeqLength()
+ * reads at FullPairwiseAlign.cpp:95-127. */
+int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, const int64_t* offsets,
+                      const int32_t* lens);
+
+/* ---- host-side helpers (no device work) ----------------------------------- */
+
+/* Per-pair integer gap penalties exactly as FullPairwiseAlign.cpp:129-148
+ * computes them (same float/double expression types). */
+int cwgpu_gap_penalties(const cwgpu_params* params, int32_t n, int32_t m, int32_t* gap_open,
+                        int32_t* gap_extend);
+/* Number of pairs the loops at FullPairwiseAlign.cpp:97 and :110 visit. */
+int64_t cwgpu_range_pair_count(int32_t nseqs, int32_t i_start, int32_t i_end, int32_t j_start,
+                               int32_t j_end);
+
+/* ---- the pairwise stage --------------------------------------------------- */
+
+/* The drop-in for pairwiseAlign(alignPtr, distMat, iStart, iEnd, jStart, jEnd)
+ * (FullPairwiseAlign.cpp:34-211): aligns every pair the reference's loops visit
+ * and stores each distance into `elements`, the packed lower-triangular double
+ * array of a SymMatrix of size nseqs+1 (SymMatrix::getElements,
+ * general/SymMatrix.h:67-71 and :166-197), at getIndex(si+1, sj+1).
+ * `dist_size` is the SymMatrix's getSize() and must equal nseqs + 1 (:47-52,
+ * else CWGPU_ERR_ARG). Pairs with an empty sequence get 1.0 like :113-118.
+ * `stats_out`, if not NULL, receives cwgpu_range_pair_count(...) entries in
+ * loop order. Returns CWGPU_ERR_RANGE for the ranges the reference rejects. */
+int cwgpu_pairwise_align(cwgpu_context* ctx, int32_t i_start, int32_t i_end, int32_t j_start,
+                         int32_t j_end, double* elements, int32_t dist_size, cwgpu_pair_stats* stats_out);
+
+/* Aligns an explicit host pair list: pairs[2q] = si (row sequence, the
+ * reference's seq1), pairs[2q+1] = sj. Writes dist_out[q] (the float the
+ * reference stores with SetAt) and, if not NULL, stats_out[q]. One persistent,
+ * graph-captured, length-ordered launch. */
+int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,
+                      cwgpu_pair_stats* stats_out);
+
+/* The same computation with one kernel launch per pair (the plain GPU form
+ * the batched form is measured against). Same outputs. */
+int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,
+                            cwgpu_pair_stats* stats_out);
+
+/* ---- plans: the pair list resident on the device, one captured launch -------
+ * A plan uploads a pair list and its load-balancing order (longest pairs
+ * first) once, owns device output arrays and holds a CUDA graph of the
+ * persistent launch, so repeated runs over resident inputs cost one
+ * cudaGraphLaunch. A plan is tied to the sequences, matrix and params that were
+ * current when it was made: after cwgpu_upload_seqs/set_params/set_matrix,
+ * cwgpu_plan_launch returns CWGPU_ERR_STATE. Plans of one context share its
+ * scratch memory and must not run concurrently. No reference counterpart: the
+ * reference re-reads its inputs for every call. */
+typedef struct cwgpu_plan cwgpu_plan;
+int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, cwgpu_plan** out);
+/* Enqueues the plan's graph on `stream` (a cudaStream_t; NULL = the context's
+ * own stream) and returns without waiting. */
+int cwgpu_plan_launch(cwgpu_plan* plan, void* stream);
+/* Waits for the device, then copies distances (and stats if not NULL) out. */
+int cwgpu_plan_results(cwgpu_plan* plan, float* dist_out, cwgpu_pair_stats* stats_out);
+/* Device address of the plan's float distance array (npairs entries). */
+void* cwgpu_plan_device_dist(cwgpu_plan* plan);
+void cwgpu_plan_destroy(cwgpu_plan* plan);
+
+/* Waits for all work of the context and reports a kernel-side error flag. */
+int cwgpu_synchronize(cwgpu_context* ctx);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* CWGPU_H */

@@ -1,0 +1,456 @@
+/*
+ * Oracle: a plain-C restatement of ClustalW 2.0.11's full (slow) pairwise
+ * distance stage, FullPairwiseAlign::pairwiseAlign
+ * (CPU/clustalw-2.0.11/src/pairwise/FullPairwiseAlign.cpp:34-660).
+ *
+ * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's
+ * CPU-baseline leg load this library, and only as the checker or the timed CPU
+ * baseline. The GPU library never links or calls it.
+ *
+ * Parity is pinned: tests/test_oracle_golden.py checks this restatement
+ * against distance matrices written by the unmodified reference
+ * (oracle/_ref/refharness) on the reference's own fixtures and on synthetic
+ * sets (tests/golden/).
+ *
+ * Differences from the reference that do not change any output:
+ *   - no `static` locals (diff() keeps them at FullPairwiseAlign.cpp:423), so
+ *     the batch entry point can run pairs on several threads;
+ *   - per-pair statistics (forward max score, end/start cells, identities,
+ *     cell counts) are returned instead of being left in members.
+ */
+#include <math.h>
+#include <pthread.h>
+#include <stdint.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define NUMRES 32
+
+typedef struct {
+    int32_t dna;            /* userParameters->getDNAFlag() */
+    float pw_gap_open;      /* getPWGapOpen() */
+    float pw_gap_extend;    /* getPWGapExtend() */
+    int32_t int_scale;      /* PairScaleValues.intScale */
+    float gap_open_scale;   /* PairScaleValues.gapOpenScale */
+    float gap_extend_scale; /* PairScaleValues.gapExtendScale */
+    int32_t mat_avg;        /* matAvg from getPairwiseMatrix */
+    int32_t gap_pos1;       /* getGapPos1() */
+    int32_t gap_pos2;       /* getGapPos2() */
+} cwo_params;
+
+typedef struct {
+    int32_t fwd_score;  /* forwardPass maxScore */
+    int32_t se1, se2;   /* forwardPass end cell */
+    int32_t sb1, sb2;   /* reversePass start cell */
+    int32_t mm_score;   /* diff() return value (FullPairwiseAlign.cpp:165) */
+    int32_t n_ident;    /* tracePath count */
+    int32_t n_match;    /* number of displ entries equal to 0 */
+    int32_t print_ptr;  /* printPtr after diff() */
+    int32_t gap_open;   /* per-pair _gapOpen */
+    int32_t gap_extend; /* per-pair _gapExtend */
+    float dist;         /* value stored with DistMatrix::SetAt */
+    int64_t cells_fwd;  /* forwardPass inner-loop iterations */
+    int64_t cells_rev;  /* reversePass inner-loop iterations (up to the break) */
+    int64_t cells_diff; /* diff() inner-loop iterations (both halves + M==1 scans) */
+} cwo_pair_result;
+
+/* Per-pair gap penalties, FullPairwiseAlign.cpp:129-148, with the same C types:
+ * the DNA branch and the extension are float expressions, the protein
+ * gap-open is a double expression with libm log(). */
+void cwo_gap_penalties(const cwo_params* p, int n, int m, int32_t* go, int32_t* ge) {
+    if (p->dna) {
+        *go = (int)(2 * p->pw_gap_open * p->int_scale * p->gap_open_scale);
+        *ge = (int)(p->pw_gap_extend * p->int_scale * p->gap_extend_scale);
+    } else {
+        int mn = n < m ? n : m;
+        if (p->mat_avg <= 0)
+            *go = 2 * (int)((p->pw_gap_open + log((double)mn)) * p->int_scale);
+        else
+            *go = (int)(2 * p->mat_avg * (p->pw_gap_open + log((double)mn)) * p->gap_open_scale);
+        *ge = (int)(p->pw_gap_extend * p->int_scale);
+    }
+}
+
+/* Work state of one pair alignment (the members of FullPairwiseAlign.h:37-59). */
+typedef struct {
+    const int32_t (*mat)[NUMRES];
+    const int8_t* s1; /* 1-based: s1[1..n] */
+    const int8_t* s2;
+    int go, ge;
+    int *HH, *DD, *RR, *SS, *displ;
+    int print_ptr, last_print;
+    int max_score, se1, se2, sb1, sb2;
+    int64_t cells_rev, cells_diff;
+    int n_match;
+} cwo_ws;
+
+static inline int score_at(const cwo_ws* w, int i, int j) { return w->mat[w->s1[i]][w->s2[j]]; }
+
+/* FullPairwiseAlign.cpp:280-341 */
+static void forward_pass(cwo_ws* w, int n, int m) {
+    int i, j, f, hh, p, t;
+    w->max_score = 0;
+    w->se1 = w->se2 = 0;
+    for (i = 0; i <= m; i++) {
+        w->HH[i] = 0;
+        w->DD[i] = -w->go;
+    }
+    for (i = 1; i <= n; i++) {
+        hh = p = 0;
+        f = -w->go;
+        for (j = 1; j <= m; j++) {
+            f -= w->ge;
+            t = hh - w->go - w->ge;
+            if (f < t) f = t;
+            w->DD[j] -= w->ge;
+            t = w->HH[j] - w->go - w->ge;
+            if (w->DD[j] < t) w->DD[j] = t;
+            hh = p + score_at(w, i, j);
+            if (hh < f) hh = f;
+            if (hh < w->DD[j]) hh = w->DD[j];
+            if (hh < 0) hh = 0;
+            p = w->HH[j];
+            w->HH[j] = hh;
+            if (hh > w->max_score) {
+                w->max_score = hh;
+                w->se1 = i;
+                w->se2 = j;
+            }
+        }
+    }
+}
+
+/* FullPairwiseAlign.cpp:343-416 */
+static void reverse_pass(cwo_ws* w) {
+    int i, j, f, hh, p, t, cost = 0;
+    w->sb1 = w->sb2 = 1;
+    for (i = w->se2; i > 0; i--) {
+        w->HH[i] = -1;
+        w->DD[i] = -1;
+    }
+    for (i = w->se1; i > 0; i--) {
+        hh = f = -1;
+        p = (i == w->se1) ? 0 : -1;
+        for (j = w->se2; j > 0; j--) {
+            w->cells_rev++;
+            f -= w->ge;
+            t = hh - w->go - w->ge;
+            if (f < t) f = t;
+            w->DD[j] -= w->ge;
+            t = w->HH[j] - w->go - w->ge;
+            if (w->DD[j] < t) w->DD[j] = t;
+            hh = p + score_at(w, i, j);
+            if (hh < f) hh = f;
+            if (hh < w->DD[j]) hh = w->DD[j];
+            p = w->HH[j];
+            w->HH[j] = hh;
+            if (hh > cost) {
+                cost = hh;
+                w->sb1 = i;
+                w->sb2 = j;
+                if (cost >= w->max_score) break;
+            }
+        }
+        if (cost >= w->max_score) break;
+    }
+}
+
+/* add/del: FullPairwiseAlign.cpp:213-224 and :614-624 */
+static void op_add(cwo_ws* w, int v) {
+    if (w->last_print < 0) {
+        w->displ[w->print_ptr - 1] = v;
+        w->displ[w->print_ptr++] = w->last_print;
+    } else {
+        w->last_print = w->displ[w->print_ptr++] = v;
+    }
+}
+
+static void op_del(cwo_ws* w, int k) {
+    if (w->last_print < 0)
+        w->last_print = w->displ[w->print_ptr - 1] -= k;
+    else
+        w->last_print = w->displ[w->print_ptr++] = -k;
+}
+
+static inline int tbgap(const cwo_ws* w, int k, int tb) { return k <= 0 ? 0 : tb + w->ge * k; }
+static inline int tegap(const cwo_ws* w, int k, int te) { return k <= 0 ? 0 : te + w->ge * k; }
+
+/* Myers-Miller linear-space alignment, FullPairwiseAlign.cpp:418-612. */
+static int diff(cwo_ws* w, int A, int B, int M, int N, int tb, int te) {
+    int type, midi, midj, i, j, midh;
+    int f, hh, e, s, t;
+    const int go = w->go, ge = w->ge;
+    int *HH = w->HH, *DD = w->DD, *RR = w->RR, *SS = w->SS;
+
+    if (N <= 0) {
+        if (M > 0) op_del(w, M);
+        return -(int)tbgap(w, M, tb);
+    }
+    if (M <= 1) {
+        if (M <= 0) {
+            op_add(w, N);
+            return -(int)tbgap(w, N, tb);
+        }
+        midh = -(tb + ge) - tegap(w, N, te);
+        hh = -(te + ge) - tbgap(w, N, tb);
+        if (hh > midh) midh = hh;
+        midj = 0;
+        for (j = 1; j <= N; j++) {
+            w->cells_diff++;
+            hh = score_at(w, A + 1, B + j) - tegap(w, N - j, te) - tbgap(w, j - 1, tb);
+            if (hh > midh) {
+                midh = hh;
+                midj = j;
+            }
+        }
+        if (midj == 0) {
+            op_del(w, 1);
+            op_add(w, N);
+        } else {
+            if (midj > 1) op_add(w, midj - 1);
+            w->displ[w->print_ptr++] = w->last_print = 0;
+            w->n_match++;
+            if (midj < N) op_add(w, N - midj);
+        }
+        return midh;
+    }
+
+    midi = M / 2;
+    HH[0] = 0;
+    t = -tb;
+    for (j = 1; j <= N; j++) {
+        HH[j] = t = t - ge;
+        DD[j] = t - go;
+    }
+    t = -tb;
+    for (i = 1; i <= midi; i++) {
+        s = HH[0];
+        HH[0] = hh = t = t - ge;
+        f = t - go;
+        for (j = 1; j <= N; j++) {
+            w->cells_diff++;
+            if ((hh = hh - go - ge) > (f = f - ge)) f = hh;
+            if ((hh = HH[j] - go - ge) > (e = DD[j] - ge)) e = hh;
+            hh = s + score_at(w, A + i, B + j);
+            if (f > hh) hh = f;
+            if (e > hh) hh = e;
+            s = HH[j];
+            HH[j] = hh;
+            DD[j] = e;
+        }
+    }
+    DD[0] = HH[0];
+
+    RR[N] = 0;
+    t = -te;
+    for (j = N - 1; j >= 0; j--) {
+        RR[j] = t = t - ge;
+        SS[j] = t - go;
+    }
+    t = -te;
+    for (i = M - 1; i >= midi; i--) {
+        s = RR[N];
+        RR[N] = hh = t = t - ge;
+        f = t - go;
+        for (j = N - 1; j >= 0; j--) {
+            w->cells_diff++;
+            if ((hh = hh - go - ge) > (f = f - ge)) f = hh;
+            if ((hh = RR[j] - go - ge) > (e = SS[j] - ge)) e = hh;
+            hh = s + score_at(w, A + i + 1, B + j + 1);
+            if (f > hh) hh = f;
+            if (e > hh) hh = e;
+            s = RR[j];
+            RR[j] = hh;
+            SS[j] = e;
+        }
+    }
+    SS[N] = RR[N];
+
+    midh = HH[0] + RR[0];
+    midj = 0;
+    type = 1;
+    for (j = 0; j <= N; j++) {
+        hh = HH[j] + RR[j];
+        if (hh >= midh)
+            if (hh > midh || (HH[j] != DD[j] && RR[j] == SS[j])) {
+                midh = hh;
+                midj = j;
+            }
+    }
+    for (j = N; j >= 0; j--) {
+        hh = DD[j] + SS[j] + go;
+        if (hh > midh) {
+            midh = hh;
+            midj = j;
+            type = 2;
+        }
+    }
+
+    if (type == 1) {
+        diff(w, A, B, midi, midj, tb, go);
+        diff(w, A + midi, B + midj, M - midi, N - midj, go, te);
+    } else {
+        diff(w, A, B, midi - 1, midj, tb, 0);
+        op_del(w, 2);
+        diff(w, A + midi + 1, B + midj, M - midi - 1, N - midj, 0, te);
+    }
+    return midh;
+}
+
+/* FullPairwiseAlign.cpp:231-278 */
+static int trace_path(const cwo_ws* w, int tsb1, int tsb2, int gap_pos1, int gap_pos2) {
+    int i1 = tsb1, i2 = tsb2, count = 0, k, i;
+    const int to_do = w->print_ptr - 1;
+    for (i = 1; i <= to_do; ++i) {
+        if (w->displ[i] == 0) {
+            int res1 = w->s1[i1], res2 = w->s2[i2];
+            if (res1 != gap_pos1 && res2 != gap_pos2 && res1 == res2) count++;
+            ++i1;
+            ++i2;
+        } else if ((k = w->displ[i]) > 0) {
+            i2 += k;
+        } else {
+            i1 -= k;
+        }
+    }
+    return count;
+}
+
+static int count_residues(const int8_t* s, int len, int g1, int g2) {
+    int c = 0;
+    for (int i = 1; i <= len; i++)
+        if (s[i] != g1 && s[i] != g2) c++;
+    return c;
+}
+
+/* One pair: the body of the sj loop, FullPairwiseAlign.cpp:112-183.
+ * s1/s2 are 0-based code arrays of length n/m. `scratch` must hold
+ * scratch_ints(maxlen) ints, maxlen >= max(n, m). */
+static size_t scratch_ints(int maxlen) { return 4 * (size_t)(2 * maxlen + 1) + 4 * (size_t)maxlen + 8; }
+
+static void align_one(const int32_t (*mat)[NUMRES], const cwo_params* p, const int8_t* s1, int n,
+                      const int8_t* s2, int m, int maxlen, int* scratch, cwo_pair_result* r) {
+    memset(r, 0, sizeof(*r));
+    cwo_gap_penalties(p, n, m, &r->gap_open, &r->gap_extend);
+    if (n == 0 || m == 0) {
+        r->dist = 1.0f;
+        return;
+    }
+    const int row = 2 * maxlen + 1;
+    cwo_ws w;
+    memset(&w, 0, sizeof(w));
+    w.mat = mat;
+    w.s1 = s1 - 1;
+    w.s2 = s2 - 1;
+    w.go = r->gap_open;
+    w.ge = r->gap_extend;
+    w.HH = scratch;
+    w.DD = scratch + row;
+    w.RR = scratch + 2 * row;
+    w.SS = scratch + 3 * row;
+    w.displ = scratch + 4 * row;
+
+    forward_pass(&w, n, m);
+    r->fwd_score = w.max_score;
+    r->se1 = w.se1;
+    r->se2 = w.se2;
+    reverse_pass(&w);
+    r->sb1 = w.sb1;
+    r->sb2 = w.sb2;
+    w.last_print = 0;
+    w.print_ptr = 1;
+    r->mm_score = diff(&w, w.sb1 - 1, w.sb2 - 1, w.se1 - w.sb1 + 1, w.se2 - w.sb2 + 1, 0, 0);
+    int count = trace_path(&w, w.sb1, w.sb2, p->gap_pos1, p->gap_pos2);
+    float mm = 100.0 * (float)count;
+    int len1 = count_residues(w.s1, n, p->gap_pos1, p->gap_pos2);
+    int len2 = count_residues(w.s2, m, p->gap_pos1, p->gap_pos2);
+    if (len1 == 0 || len2 == 0)
+        mm = 0;
+    else
+        mm /= (float)(len1 < len2 ? len1 : len2);
+    r->dist = ((float)100.0 - mm) / (float)100.0;
+    r->n_ident = count;
+    r->n_match = w.n_match;
+    r->print_ptr = w.print_ptr;
+    r->cells_fwd = (int64_t)n * m;
+    r->cells_rev = w.cells_rev;
+    r->cells_diff = w.cells_diff;
+}
+
+/* ---------------------------------------------------------------- batch API */
+
+typedef struct {
+    const int8_t* codes;
+    const int64_t* offsets;
+    const int32_t* lens;
+    const int32_t (*mat)[NUMRES];
+    const cwo_params* p;
+    const int32_t* pairs;
+    int64_t npairs;
+    cwo_pair_result* out;
+    int maxlen;
+    int64_t next;
+    pthread_mutex_t mu;
+} cwo_job;
+
+static void* worker(void* arg) {
+    cwo_job* j = (cwo_job*)arg;
+    int* scratch = (int*)malloc(sizeof(int) * scratch_ints(j->maxlen));
+    if (!scratch) return (void*)1;
+    for (;;) {
+        pthread_mutex_lock(&j->mu);
+        int64_t lo = j->next;
+        j->next += 16;
+        pthread_mutex_unlock(&j->mu);
+        if (lo >= j->npairs) break;
+        int64_t hi = lo + 16 < j->npairs ? lo + 16 : j->npairs;
+        for (int64_t q = lo; q < hi; q++) {
+            int a = j->pairs[2 * q], b = j->pairs[2 * q + 1];
+            align_one(j->mat, j->p, j->codes + j->offsets[a], j->lens[a], j->codes + j->offsets[b],
+                      j->lens[b], j->maxlen, scratch, &j->out[q]);
+        }
+    }
+    free(scratch);
+    return 0;
+}
+
+/* Aligns the listed pairs (pairs[2q] = row sequence si, pairs[2q+1] = column
+ * sequence sj, 0-based) with `nthreads` threads. Returns 0 on success. */
+int cwo_align_pairs(const int8_t* codes, const int64_t* offsets, const int32_t* lens, int32_t nseqs,
+                    const int32_t* matrix, const cwo_params* p, const int32_t* pairs, int64_t npairs,
+                    cwo_pair_result* out, int32_t nthreads) {
+    cwo_job j;
+    int maxlen = 1;
+    for (int s = 0; s < nseqs; s++)
+        if (lens[s] > maxlen) maxlen = lens[s];
+    for (int64_t q = 0; q < npairs; q++) {
+        if (pairs[2 * q] < 0 || pairs[2 * q] >= nseqs || pairs[2 * q + 1] < 0 || pairs[2 * q + 1] >= nseqs)
+            return 1;
+    }
+    j.codes = codes;
+    j.offsets = offsets;
+    j.lens = lens;
+    j.mat = (const int32_t (*)[NUMRES])matrix;
+    j.p = p;
+    j.pairs = pairs;
+    j.npairs = npairs;
+    j.out = out;
+    j.maxlen = maxlen;
+    j.next = 0;
+    pthread_mutex_init(&j.mu, 0);
+    if (nthreads < 1) nthreads = 1;
+    if (nthreads > 512) nthreads = 512;
+    pthread_t th[512];
+    int started = 0, rc = 0;
+    for (int t = 1; t < nthreads; t++) {
+        if (pthread_create(&th[started], 0, worker, &j) == 0) started++;
+    }
+    if (worker(&j)) rc = 2;
+    for (int t = 0; t < started; t++) {
+        void* ret = 0;
+        pthread_join(th[t], &ret);
+        if (ret) rc = 2;
+    }
+    pthread_mutex_destroy(&j.mu);
+    return rc;
+}

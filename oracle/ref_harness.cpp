@@ -1,0 +1,133 @@
+// Reference harness: links the UNMODIFIED ClustalW 2.0.11 CPU objects (built from
+// the reference tree by oracle/build_ref.sh, outputs only under oracle/_ref/) and
+// runs clustalw::FullPairwiseAlign::pairwiseAlign on one FASTA file.
+//
+// TEST INFRASTRUCTURE ONLY. This program is the reference itself, used to pin the
+// oracle restatement (oracle/oracle.c) and to write the golden fixtures under
+// tests/golden/. Nothing in the shipped library calls it.
+//
+// It mirrors what Clustal::align does before the pairwise stage
+// (CPU/clustalw-2.0.11/src/Clustal.cpp:129-162): sequence input through
+// FileReader::readSeqs (Clustal.cpp:1051-1059), setDNAParams/setProtParams,
+// DistMatrix sized numSeqs+1, then one pairwiseAlign(iStart, iEnd, jStart, jEnd).
+//
+// Usage: refharness IN.fa OUT.bin [iStart iEnd jStart jEnd]
+//
+// OUT.bin layout (little endian):
+//   char[8]  "CWREF01\0"
+//   int32    nseqs, dna_flag, int_scale, mat_avg, gap_pos1, gap_pos2, max_aln_length
+//   float    pw_gap_open, pw_gap_extend, gap_open_scale, gap_extend_scale
+//   int32    matrix[32*32]          (SubMatrix::getPairwiseMatrix output)
+//   int32    lens[nseqs]
+//   int32    codes[sum(lens)]       (SeqArray rows 1..nseqs, elements 1..len)
+//   int32    range[4]               (iStart, iEnd, jStart, jEnd)
+//   double   elements[(N+1)(N+2)/2] (SymMatrix::getElements, packed lower triangle)
+//   double   seconds                (wall time of pairwiseAlign)
+#include <chrono>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "alignment/Alignment.h"
+#include "fileInput/FileReader.h"
+#include "general/DebugLog.h"
+#include "general/Stats.h"
+#include "general/UserParameters.h"
+#include "general/Utility.h"
+#include "general/clustalw.h"
+#include "pairwise/FullPairwiseAlign.h"
+#include "substitutionMatrix/SubMatrix.h"
+
+namespace clustalw {
+UserParameters* userParameters;
+Utility* utilityObject;
+SubMatrix* subMatrix;
+DebugLog* logObject;
+Stats* statsObject;
+}  // namespace clustalw
+
+using namespace clustalw;
+
+static void put(FILE* f, const void* p, size_t n) {
+    if (n && fwrite(p, 1, n, f) != n) {
+        fprintf(stderr, "refharness: short write\n");
+        exit(2);
+    }
+}
+
+int main(int argc, char** argv) {
+    if (argc != 3 && argc != 7) {
+        fprintf(stderr, "usage: %s IN.fa OUT.bin [iStart iEnd jStart jEnd]\n", argv[0]);
+        return 2;
+    }
+    userParameters = new UserParameters(false);
+    utilityObject = new Utility();
+    subMatrix = new SubMatrix();
+    statsObject = new Stats();
+    userParameters->setDisplayInfo(false);
+    userParameters->setSeqName(std::string(argv[1]));
+
+    Alignment aln;
+    FileReader reader;
+    int code = reader.readSeqs(&aln, 1);
+    if (code != OK) {
+        fprintf(stderr, "refharness: readSeqs failed with code %d\n", code);
+        return 3;
+    }
+    if (userParameters->getDNAFlag())
+        userParameters->setDNAParams();
+    else
+        userParameters->setProtParams();
+
+    const int n = aln.getNumSeqs();
+    int range[4] = {0, n, 0, n};
+    if (argc == 7)
+        for (int k = 0; k < 4; ++k) range[k] = atoi(argv[3 + k]);
+
+    SymMatrix dist;
+    dist.ResizeRect(n + 1);
+
+    FullPairwiseAlign fpa;
+    auto t0 = std::chrono::steady_clock::now();
+    fpa.pairwiseAlign(&aln, &dist, range[0], range[1], range[2], range[3]);
+    auto t1 = std::chrono::steady_clock::now();
+    double secs = std::chrono::duration<double>(t1 - t0).count();
+
+    int matrix[NUMRES][NUMRES];
+    PairScaleValues scale;
+    int mat_avg = 0;
+    subMatrix->getPairwiseMatrix(matrix, scale, mat_avg);
+
+    FILE* f = fopen(argv[2], "wb");
+    if (!f) {
+        fprintf(stderr, "refharness: cannot open %s\n", argv[2]);
+        return 4;
+    }
+    put(f, "CWREF01\0", 8);
+    int hdr[7] = {n,
+                  userParameters->getDNAFlag() ? 1 : 0,
+                  scale.intScale,
+                  mat_avg,
+                  userParameters->getGapPos1(),
+                  userParameters->getGapPos2(),
+                  aln.getMaxAlnLength()};
+    put(f, hdr, sizeof(hdr));
+    float fl[4] = {userParameters->getPWGapOpen(), userParameters->getPWGapExtend(),
+                   scale.gapOpenScale, scale.gapExtendScale};
+    put(f, fl, sizeof(fl));
+    put(f, matrix, sizeof(matrix));
+    std::vector<int> lens(n);
+    for (int s = 0; s < n; ++s) lens[s] = aln.getSeqLength(s + 1);
+    put(f, lens.data(), sizeof(int) * n);
+    const SeqArray* sa = aln.getSeqArray();
+    for (int s = 0; s < n; ++s) put(f, (*sa)[s + 1].data() + 1, sizeof(int) * lens[s]);
+    put(f, range, sizeof(range));
+    size_t nel = (size_t)(n + 1) * (n + 2) / 2;
+    put(f, dist.getElements(), sizeof(double) * nel);
+    put(f, &secs, sizeof(secs));
+    fclose(f);
+    printf("refharness: %d seqs, dna=%d, pairwise %.6f s\n", n, hdr[1], secs);
+    return 0;
+}

@@ -1,0 +1,68 @@
+import os
+import sys
+
+import numpy as np
+import pytest
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+for p in (REPO, os.path.join(REPO, "cuda-clustalw_gb300")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+GOLDEN = os.path.join(REPO, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300); run with -m gpu")
+
+
+def load_golden(name):
+    """A golden fixture written by tests/golden/make_golden.py from the reference."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    lens = z["lens"]
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64) if len(lens) else np.zeros(0, np.int64)
+    seqs = [z["codes"][o : o + L].astype(np.int8) for o, L in zip(offs, lens)]
+    pi, pf = z["params_int"], z["params_float"]
+    params = dict(
+        dna=int(pi[0]),
+        int_scale=int(pi[1]),
+        mat_avg=int(pi[2]),
+        gap_pos1=int(pi[3]),
+        gap_pos2=int(pi[4]),
+        pw_gap_open=float(pf[0]),
+        pw_gap_extend=float(pf[1]),
+        gap_open_scale=float(pf[2]),
+        gap_extend_scale=float(pf[3]),
+    )
+    return dict(
+        name=name,
+        seqs=seqs,
+        matrix=z["matrix"],
+        params=params,
+        range=tuple(int(x) for x in z["range"]),
+        elements=z["elements"],
+    )
+
+
+def golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def range_pairs(n, i0, i1, j0, j1):
+    out = [(si, sj) for si in range(max(0, i0), min(n, i1)) for sj in range(max(si + 1, j0 + 1), min(n, j1))]
+    return np.array(out, dtype=np.int32).reshape(-1, 2)
+
+
+def sym_index(pairs):
+    """SymMatrix::getIndex for 1-based (si+1, sj+1), si < sj."""
+    i = pairs[:, 0].astype(np.int64)
+    j = pairs[:, 1].astype(np.int64)
+    return (j * (j + 1)) // 2 + i
+
+
+@pytest.fixture(scope="session")
+def oracle_mod():
+    from oracle import oracle as O
+
+    O.build()
+    return O

@@ -1,0 +1,117 @@
+"""Writes the golden fixtures under tests/golden/ by running the UNMODIFIED
+reference (ClustalW 2.0.11 FullPairwiseAlign, built by oracle/build_ref.sh)
+through oracle/_ref/refharness.
+
+Run from the repository root, where the reference tree is available:
+    python tests/golden/make_golden.py
+
+Each <name>.npz holds the encoded sequences exactly as the reference's reader
+produced them, the pairwise matrix and scalars the reference used, the range,
+and the reference's full packed DistMatrix (double). It also refreshes
+cuda-clustalw_gb300/clustalw_gb300/data/pairwise_matrices.json (the default
+protein and DNA pairwise matrices).
+"""
+import json
+import os
+import sys
+import tempfile
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "cuda-clustalw_gb300"))
+
+from clustalw_gb300 import synth  # noqa: E402
+from oracle import oracle as O  # noqa: E402
+
+FIXTURES = "/root/reference/test_data/correct"
+OUT = os.path.dirname(os.path.abspath(__file__))
+
+
+def save(name, ref):
+    seqs = ref["seqs"]
+    lens = np.array([len(s) for s in seqs], dtype=np.int32)
+    codes = np.concatenate(seqs).astype(np.int8) if len(seqs) else np.zeros(0, np.int8)
+    p = ref["params"]
+    np.savez_compressed(
+        os.path.join(OUT, name + ".npz"),
+        codes=codes,
+        lens=lens,
+        matrix=ref["matrix"].astype(np.int32),
+        params_int=np.array([p["dna"], p["int_scale"], p["mat_avg"], p["gap_pos1"], p["gap_pos2"]], np.int32),
+        params_float=np.array(
+            [p["pw_gap_open"], p["pw_gap_extend"], p["gap_open_scale"], p["gap_extend_scale"]], np.float32
+        ),
+        range=ref["range"].astype(np.int32),
+        elements=ref["elements"],
+        max_aln_length=np.int32(ref["max_aln_length"]),
+    )
+    print(f"{name}: {ref['n']} seqs, range {list(ref['range'])}, ref {ref['seconds']:.2f}s")
+
+
+def run_fasta(text, name, rng=None):
+    with tempfile.TemporaryDirectory() as d:
+        fa = os.path.join(d, name + ".fa")
+        with open(fa, "w") as f:
+            f.write(text)
+        return O.run_reference(fa, os.path.join(d, "out.bin"), rng)
+
+
+def main():
+    O.build()
+    mats = {}
+    for fx in ["100_97", "100_498", "100_1002", "100_1523"]:
+        with tempfile.TemporaryDirectory() as d:
+            ref = O.run_reference(os.path.join(FIXTURES, fx + ".fa"), os.path.join(d, "o.bin"))
+        save("fixture_" + fx, ref)
+        kind = "dna" if ref["params"]["dna"] else "protein"
+        mats.setdefault(kind, {"matrix": ref["matrix"].reshape(-1).tolist(), "params": ref["params"]})
+        if fx == "100_97":
+            n = ref["n"]
+            # Partial ranges, as Clustal::sequencesAlignToProfile (Clustal.cpp:404-416) and
+            # other callers pass them (FullPairwiseAlign.cpp:97,110).
+            for tag, rng in [("cols49", (0, n, 49, n)), ("rows10_30", (10, 30, 0, n)), ("block", (20, 60, 40, 70))]:
+                with tempfile.TemporaryDirectory() as d:
+                    r2 = O.run_reference(os.path.join(FIXTURES, fx + ".fa"), os.path.join(d, "o.bin"), rng)
+                save(f"range_{fx}_{tag}", r2)
+
+    save("synth_protein_60x97", run_fasta(synth.to_fasta(synth.protein_family(60, 97, 11)), "p"))
+    save("synth_dna_40x300", run_fasta(synth.to_fasta(synth.dna_family(40, 300, 12)), "d"))
+    uneven = []
+    for f, L in enumerate([5, 30, 170, 600]):
+        uneven += synth.protein_family(10, L, 100 + f)
+    save("synth_uneven_40", run_fasta(synth.to_fasta(uneven), "u"))
+    save("synth_long_6x3000", run_fasta(synth.to_fasta(synth.protein_family(6, 3000, 13)), "l"))
+
+    # Edge cases: length-1 and length-2 sequences, identical sequences, runs
+    # that create ties, internal gaps, an all-gap sequence, ambiguity codes,
+    # and a short-vs-long pair.
+    edge = [
+        "W",
+        "MA",
+        "MKTAYIAKQRQISFVKSHFSRQ",
+        "MKTAYIAKQRQISFVKSHFSRQ",
+        "AAAAAAAAAAAAAAAAAAAA",
+        "AAAAAAAAAAGAAAAAAAAA",
+        "MK--LVAG-HHW",
+        "----",
+        "XXXXBZBZXX",
+        "GGGGGGGG",
+        "KR",
+        "ACDEFGHIKLMNPQRSTVWY" * 12,
+        "WWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWW",
+        "MSLLTEVETPTRNGWECKCSDSSD",
+        "P",
+    ]
+    text = "".join(f">e{i}\n{s}\n" for i, s in enumerate(edge))
+    save("edge_protein", run_fasta(text, "e"))
+
+    os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
+    with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
+        json.dump(mats, f, indent=0)
+    print("wrote pairwise_matrices.json with", sorted(mats))
+
+
+if __name__ == "__main__":
+    main()

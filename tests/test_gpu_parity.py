@@ -1,0 +1,90 @@
+"""GPU parity: the sm_103a kernels, called through the C ABI, against the
+reference's distance matrices (golden fixtures, bit-exact) and against the
+oracle's per-pair intermediates (forward max score, end cell, start cell,
+Myers-Miller score, identity and match counts)."""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden, range_pairs, sym_index
+
+pytestmark = pytest.mark.gpu
+
+STAT_FIELDS = ["fwd_score", "se1", "se2", "sb1", "sb2", "mm_score", "n_ident", "n_match"]
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    from clustalw_gb300 import native
+
+    c = native.Context(0)
+    yield c
+    c.close()
+
+
+def setup(ctx, g):
+    ctx.set_matrix(g["matrix"])
+    ctx.set_params(g["params"])
+    ctx.upload_seqs(g["seqs"])
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_distmatrix_bit_exact_vs_reference(ctx, name):
+    g = load_golden(name)
+    setup(ctx, g)
+    n = len(g["seqs"])
+    elements = np.zeros_like(g["elements"])
+    ctx.pairwise_align(*g["range"], elements, n + 1)
+    bad = np.nonzero(elements != g["elements"])[0]
+    assert len(bad) == 0, f"{name}: {len(bad)} of {len(elements)} entries differ, first {bad[:5]}"
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_pair_stats_vs_oracle(ctx, oracle_mod, name):
+    g = load_golden(name)
+    setup(ctx, g)
+    pairs = range_pairs(len(g["seqs"]), *g["range"])
+    if len(pairs) == 0:
+        pytest.skip("empty range")
+    dist, st = ctx.align_pairs(pairs, stats=True)
+    want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    assert np.array_equal(dist, want["dist"])
+    for f in STAT_FIELDS:
+        bad = np.nonzero(st[f] != want[f])[0]
+        assert len(bad) == 0, f"{name}.{f}: {len(bad)} pairs differ, e.g. pair {pairs[bad[0]]}: gpu {st[f][bad[0]]} oracle {want[f][bad[0]]}"
+
+
+def test_plain_form_matches_batched(ctx):
+    g = load_golden("synth_uneven_40")
+    setup(ctx, g)
+    pairs = range_pairs(len(g["seqs"]), 0, 40, 0, 40)[::7]
+    d1, s1 = ctx.align_pairs(pairs, stats=True)
+    d2, s2 = ctx.align_pairs(pairs, stats=True, plain=True)
+    assert np.array_equal(d1, d2)
+    assert np.array_equal(s1, s2)
+
+
+def test_plan_replay_is_idempotent(ctx):
+    g = load_golden("synth_protein_60x97")
+    setup(ctx, g)
+    pairs = range_pairs(60, 0, 60, 0, 60)
+    plan = ctx.plan(pairs)
+    plan.launch()
+    a = plan.results()
+    plan.launch()
+    plan.launch()
+    b = plan.results()
+    plan.close()
+    assert np.array_equal(a, b)
+
+
+def test_swapped_pair_order(ctx, oracle_mod):
+    """(sj, si) is a different alignment problem (seq1/seq2 roles swap); both
+    orders must match the oracle."""
+    g = load_golden("synth_uneven_40")
+    setup(ctx, g)
+    pairs = range_pairs(40, 0, 40, 0, 40)[:200][:, ::-1].copy()
+    dist, st = ctx.align_pairs(pairs, stats=True)
+    want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    assert np.array_equal(dist, want["dist"])
+    for f in STAT_FIELDS:
+        assert np.array_equal(st[f], want[f]), f

@@ -1,0 +1,64 @@
+"""CPU-side checks of the C ABI: the library builds for sm_103a, loads, exports
+every function include/cwgpu.h declares, and its host-only helpers (no device
+work) agree with the oracle."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import REPO, load_golden
+
+
+def declared_functions():
+    text = open(os.path.join(REPO, "include", "cwgpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(cwgpu_\w+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from clustalw_gb300 import native
+
+    return native.load()
+
+
+def test_header_declares_core_entry_points():
+    names = declared_functions()
+    for must in ["cwgpu_create", "cwgpu_pairwise_align", "cwgpu_align_pairs", "cwgpu_align_pairs_plain", "cwgpu_plan_create"]:
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lib):
+    from clustalw_gb300 import native
+
+    for name in declared_functions():
+        assert hasattr(lib, name), f"{name} declared in cwgpu.h but not exported"
+        assert name in native.SIGNATURES, f"{name} has no ctypes signature"
+
+
+def test_gap_penalties_match_oracle(lib, oracle_mod):
+    from clustalw_gb300 import native
+
+    for g in ["fixture_100_97", "fixture_100_1002", "synth_uneven_40"]:
+        p = load_golden(g)["params"]
+        for n, m in [(1, 1), (2, 7), (97, 96), (498, 498), (1523, 1600), (3000, 2999), (65535, 65535)]:
+            assert native.gap_penalties(p, n, m) == oracle_mod.gap_penalties(p, n, m)
+    # matAvg <= 0 protein branch (2 * (int)(...)).
+    p = dict(load_golden("fixture_100_97")["params"], mat_avg=0)
+    for n in [5, 50, 500]:
+        assert native.gap_penalties(p, n, n) == oracle_mod.gap_penalties(p, n, n)
+
+
+def test_range_pair_count(lib):
+    from clustalw_gb300 import native
+    from conftest import range_pairs
+
+    for rng in [(0, 10, 0, 10), (0, 10, 4, 10), (3, 7, 0, 10), (5, 5, 0, 10), (0, 100, 0, 100), (8, 20, 9, 30)]:
+        assert native.range_pair_count(10, *rng) == len(range_pairs(10, *rng))
+
+
+def test_status_strings(lib):
+    for code in range(10):
+        assert lib.cwgpu_status_string(code)
