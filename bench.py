@@ -1,0 +1,455 @@
+#!/usr/bin/env python
+"""Benchmark of the GB300 full-pairwise distance stage (ClustalW 2.0.11
+FullPairwiseAlign::pairwiseAlign, all N(N-1)/2 pairs of a sequence set).
+
+One step = one pass of the stage over one synthetic sequence family
+(default: 1000 protein sequences from a root of length 1523, 499,500 pairs,
+Gonnet, gap open 10.0, extension 0.1). Metric: GCUPS = sum over pairs of n*m
+divided by the time of the step.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl ours (default) prints one JSON line with
+  value      device-resident form: inputs uploaded and the pair plan built
+             before timing; K graph launches timed with CUDA events on the
+             launching stream, L2 flushed between steps
+  e2e        the same through the C ABI with host buffers: cwgpu_upload_seqs +
+             cwgpu_align_pairs (pair list in, distances out) per step
+  roofline   INT32-issue roofline of the one kernel (k_pairwise)
+  cpu_baseline  the oracle restatement on the host cores, bounded sample
+  plain      the one-launch-per-pair GPU form on a sample of the same pairs
+--impl reference times the reference CPU algorithm (the oracle port; the
+reference's own build is not available on the GPU host) on all host threads.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+for _p in (REPO, os.path.join(REPO, "cuda-clustalw_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+OPS_PER_CELL = 8  # E, F via __viaddmax (2), H-gap term (1), diag add + 3-way max (2), max tracking (2), score (1)
+INT32_LANES_PER_SM = 128
+
+WORKLOADS = {
+    # name: (kind, generator args)
+    "protein-1000x1523": ("protein", dict(nseqs=1000, root_len=1523)),
+    "protein-100x97": ("protein", dict(nseqs=100, root_len=97)),
+    "dna-2000x1000": ("dna", dict(nseqs=2000, root_len=1000)),
+    "protein-uneven-8x125": ("protein", dict(uneven=True)),
+}
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--workload", default="protein-1000x1523", choices=sorted(WORKLOADS))
+    ap.add_argument("--seed", type=int, default=1)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="CPU-baseline sample budget")
+    ap.add_argument("--plain-pairs", type=int, default=64, help="pairs timed in the plain per-pair form")
+    ap.add_argument("--e2e-steps", type=int, default=3)
+    ap.add_argument("--nseqs", type=int, default=0, help="smaller case of the same family model (profiling)")
+    ap.add_argument("--device-only", action="store_true", help="time only the device-resident form (profiling)")
+    return ap.parse_args()
+
+
+def make_workload(name, seed, nseqs=0):
+    from clustalw_gb300 import load_matrix, synth
+
+    kind, a = WORKLOADS[name]
+    if a.get("uneven"):
+        seqs = synth.uneven_protein(8, 125, 30, 2000, seed)
+    elif kind == "dna":
+        seqs = synth.dna_family(nseqs or a["nseqs"], a["root_len"], seed)
+    else:
+        seqs = synth.protein_family(nseqs or a["nseqs"], a["root_len"], seed)
+    matrix, params = load_matrix(kind)
+    return seqs, matrix, params
+
+
+def nm_cells(seqs, pairs):
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    return int((lens[pairs[:, 0]] * lens[pairs[:, 1]]).sum())
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", str(rank)))
+    return rank, world, local
+
+
+# ---------------------------------------------------------------- clocks
+
+
+class ClockSampler:
+    """nvidia-smi samples (200 ms) of SM clock and throttle reasons while running."""
+
+    FIELDS = (
+        "uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+        "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+        "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap"
+    )
+
+    def __init__(self, uuid):
+        self.uuid = uuid
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.out = open(self.path, "w")
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.out,
+                stderr=subprocess.DEVNULL,
+            )
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.out.close()
+
+    def summary(self):
+        if self.proc is None or not self.path:
+            return None
+        sms, maxs, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as f:
+            for line in f:
+                parts = [p.strip() for p in line.split(",")]
+                if len(parts) < 9 or (self.uuid and parts[0] != self.uuid):
+                    continue
+                try:
+                    sms.append(float(parts[1]))
+                    maxs.append(float(parts[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, parts[5:9]):
+                    if v.lower().startswith("active"):
+                        reasons.add(nm)
+        os.unlink(self.path)
+        if not sms:
+            return None
+        return {"sm_mhz": statistics.median(sms), "sm_max_mhz": max(maxs), "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# ---------------------------------------------------------------- CPU legs
+
+
+def run_cpu(seqs, matrix, params, pairs, threads):
+    from oracle import oracle
+
+    t = time.perf_counter()
+    res = oracle.align_pairs(seqs, matrix, params, pairs, nthreads=threads)
+    return time.perf_counter() - t, res
+
+
+def cpu_baseline(seqs, matrix, params, pairs, seconds, seed=0):
+    """GCUPS of the oracle restatement (port of the reference CPU algorithm) on a
+    bounded uniform sample of the workload's pairs, all host threads."""
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(seed)
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    mean_nm = float((lens[pairs[:, 0]] * lens[pairs[:, 1]]).mean())
+    perm = rng.permutation(len(pairs))
+    used, total_t, total_c, chunk = 0, 0.0, 0, 4 * threads
+    while total_t < 0.9 * seconds and used < len(pairs):
+        sample = pairs[np.sort(perm[used : used + chunk])]
+        dt, _ = run_cpu(seqs, matrix, params, sample, threads)
+        used += len(sample)
+        total_t += dt
+        total_c += nm_cells(seqs, sample)
+        rate = total_c / max(total_t, 1e-9)
+        chunk = int(max(threads, min(len(pairs), rate * max(0.5, seconds - total_t) / mean_nm)))
+    return {
+        "value": total_c / total_t / 1e9,
+        "unit": "GCUPS",
+        "cores": threads,
+        "kind": "port",
+        "sample": f"{used} of {len(pairs)} pairs (seeded uniform), {total_t:.1f} s on {threads} threads",
+    }
+
+
+def reference_arm(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    seqs, matrix, params = make_workload(args.workload, args.seed, args.nseqs)
+    from clustalw_gb300 import synth
+
+    pairs = synth.all_pairs(len(seqs))
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(12345)
+    lens = np.array([len(s) for s in seqs], dtype=np.int64)
+    # Calibrate the per-step sample so that all W+K steps take about 2 minutes.
+    calib = pairs[rng.choice(len(pairs), size=min(len(pairs), 8 * threads), replace=False)]
+    dt, _ = run_cpu(seqs, matrix, params, calib, threads)
+    rate = nm_cells(seqs, calib) / max(dt, 1e-6)
+    per_step = 120.0 / max(1, args.steps + args.warmup)
+    mean_nm = float((lens[pairs[:, 0]] * lens[pairs[:, 1]]).mean())
+    k = int(min(len(pairs), max(threads, rate * per_step / mean_nm)))
+    times, cells = [], []
+    for step in range(args.warmup + args.steps):
+        sample = pairs[np.sort(rng.choice(len(pairs), size=k, replace=False))]
+        dt, _ = run_cpu(seqs, matrix, params, sample, threads)
+        if step >= args.warmup:
+            times.append(dt)
+            cells.append(nm_cells(seqs, sample))
+    value = sum(cells) / sum(times) / 1e9
+    line = {
+        "impl": "reference",
+        "metric": "GCUPS",
+        "value": value,
+        "unit": "GCUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": 1e3 * sum(times) / len(times),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded tree-evolved family)",
+        "config": {"workload": args.workload, "pairs": int(len(pairs)), "sample_pairs_per_step": k},
+        "cpu_baseline": {
+            "value": value,
+            "unit": "GCUPS",
+            "cores": threads,
+            "kind": "port",
+            "sample": f"{k} seeded uniform pairs per step of {len(pairs)}; oracle/oracle.c restatement of "
+            "FullPairwiseAlign (the reference build needs its source tree, absent on the GPU host)",
+        },
+        "e2e": {"value": value, "unit": "GCUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(REPO, "MEASURED_PEAKS.json")) as f:
+            return json.load(f)
+    except OSError:
+        return {}
+
+
+def traffic_per_cell():
+    """DRAM bytes per forward cell from the committed ncu summary, if any."""
+    path = os.path.join(REPO, "profiles", "k_pairwise_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["dram_bytes_per_nm_cell"]), d.get("source", path)
+    except (OSError, KeyError, ValueError):
+        return None, None
+
+
+def ours_arm(args):
+    import torch
+
+    from clustalw_gb300 import native, synth
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    seqs, matrix, params = make_workload(args.workload, args.seed + rank, args.nseqs)
+    pairs = synth.all_pairs(len(seqs))
+    cells_nm = nm_cells(seqs, pairs)
+    packed = native.pack_sequences(seqs)
+
+    ctx = native.Context(local)
+    ctx.set_matrix(matrix)
+    ctx.set_params(params)
+    ctx.upload_seqs(packed=packed)
+    plan = ctx.plan(pairs)
+    # A dedicated stream: the graph is launched on it and the CUDA events are
+    # recorded on it (torch's default stream has handle 0, which the C ABI
+    # reads as "the context's own stream").
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+
+    for _ in range(args.warmup):
+        plan.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    fwd, rev, dif = plan.cell_counts()
+    ref_dist = plan.results()
+
+    uuid = getattr(torch.cuda.get_device_properties(local), "uuid", None)
+    uuid = None if uuid is None else (str(uuid) if str(uuid).startswith("GPU-") else "GPU-" + str(uuid))
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(uuid) as clk:
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record(stream)
+            plan.launch(stream.cuda_stream)
+            ends[k].record(stream)
+        torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = sum(step_ms) / 1e3
+    if world > 1:
+        t = torch.tensor([total_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_s = float(t.item())
+    dist_out = plan.results()
+    if not np.array_equal(dist_out, ref_dist):
+        raise RuntimeError("distances changed between runs")
+    ms = 1e3 * total_s / args.steps
+    value = world * cells_nm * args.steps / total_s / 1e9
+    if args.device_only:
+        if rank == 0:
+            print(json.dumps({"metric": "GCUPS", "value": value, "ms_per_step": ms, "pairs": int(len(pairs)),
+                              "cells": [fwd, rev, dif], "device_only": True}), flush=True)
+        plan.close()
+        ctx.close()
+        return
+
+    # End to end through the C ABI with host buffers.
+    e2e_times = []
+    torch.cuda.set_stream(torch.cuda.default_stream())
+    for k in range(args.e2e_steps + 1):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        ctx.upload_seqs(packed=packed)
+        d = ctx.align_pairs(pairs)
+        e2e_times.append(time.perf_counter() - t)
+        if k == 0 and not np.array_equal(d, ref_dist):
+            raise RuntimeError("e2e distances differ from the device-resident run")
+    e2e_s = statistics.mean(e2e_times[1:])
+    lmax = int(packed[2].max()) if len(packed[2]) else 0
+    codes_padded = int(sum((int(L) + 15) & ~15 for L in packed[2]))
+    h2d = codes_padded + 8 * len(seqs) + 4 * len(seqs) + 4 * len(seqs) + 4 * (lmax + 1) + 4 * 1024
+    h2d += 8 * len(pairs) + 4 * len(pairs)
+    d2h = 4 * len(pairs) + 4  # distances + the kernel status word
+
+    # Plain one-launch-per-pair form on a seeded sample of the same pairs.
+    rng = np.random.default_rng(7)
+    ps = pairs[np.sort(rng.choice(len(pairs), size=min(args.plain_pairs, len(pairs)), replace=False))]
+    ctx.align_pairs(ps[:2], plain=True)
+    t = time.perf_counter()
+    d_plain = ctx.align_pairs(ps, plain=True)
+    plain_s = time.perf_counter() - t
+    # Same pairs through the batched form: must agree bit for bit.
+    if not np.array_equal(d_plain, ctx.align_pairs(ps)):
+        raise RuntimeError("plain and batched forms disagree")
+    plain_gcups = nm_cells(seqs, ps) / plain_s / 1e9
+
+    peaks = measured_peaks()
+    props = torch.cuda.get_device_properties(local)
+    sm_max = float(peaks.get("sm_max_mhz", 2070.0))
+    peak_tops = props.multi_processor_count * INT32_LANES_PER_SM * sm_max * 1e6 / 1e12
+    cells_alg = fwd + rev + dif
+    achieved = cells_alg * OPS_PER_CELL / (ms / 1e3) / 1e12
+    tpc, tsrc = traffic_per_cell()
+    roofline = {
+        "bound": "int32",
+        "achieved": achieved,
+        "peak": peak_tops,
+        "unit": "Tops/s",
+        "frac": achieved / peak_tops,
+        "traffic": (tpc * cells_nm) if tpc is not None else None,
+        "kernel": "k_pairwise",
+        "cells_per_launch": {"forward": fwd, "reverse": rev, "diff": dif, "total": cells_alg},
+        "ops_per_cell": OPS_PER_CELL,
+        "peak_source": f"{props.multi_processor_count} SMs x {INT32_LANES_PER_SM} INT32 lanes x "
+        f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
+        "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        "traffic_source": tsrc,
+    }
+
+    line = {
+        "metric": "GCUPS",
+        "value": value,
+        "unit": "GCUPS",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "int32",
+        "data": "synthetic (seeded tree-evolved family)",
+        "config": {
+            "workload": args.workload,
+            "nseqs": len(seqs),
+            "pairs": int(len(pairs)),
+            "mean_len": float(np.mean(packed[2])),
+            "matrix": "gonnet" if params["dna"] == 0 else "iub",
+            "form": "batched: persistent graph-captured launch, longest pairs first",
+            "l2": "flushed between timed steps (256 MiB write, untimed)",
+            "pairs_per_s": len(pairs) * world / (ms / 1e3),
+        },
+        "e2e": {
+            "value": cells_nm / e2e_s / 1e9,
+            "unit": "GCUPS",
+            "h2d_bytes_per_step": h2d,
+            "d2h_bytes_per_step": d2h,
+            "ms_per_step": 1e3 * e2e_s,
+            "call": "cwgpu_upload_seqs + cwgpu_align_pairs (host pair list in, host distances out)",
+        },
+        "plain": {
+            "value": plain_gcups,
+            "unit": "GCUPS",
+            "sample": f"{len(ps)} pairs, one kernel launch per pair",
+            "batched_over_plain": value / world / plain_gcups,
+        },
+        "roofline": roofline,
+        "gpu_launches": args.steps,
+    }
+    if rank == 0:
+        clocks = clk.summary()
+        if clocks:
+            line["clocks"] = clocks
+        if world == 1:
+            line["cpu_baseline"] = cpu_baseline(seqs, matrix, params, pairs, args.cpu_seconds)
+        print(json.dumps(line), flush=True)
+    plan.close()
+    ctx.close()
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    args = parse_args()
+    if args.impl == "reference":
+        reference_arm(args)
+    else:
+        ours_arm(args)
+
+
+if __name__ == "__main__":
+    main()

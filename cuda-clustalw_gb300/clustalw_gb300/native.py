@@ -96,6 +96,7 @@ SIGNATURES = {
     "cwgpu_plan_launch": (ctypes.c_int, [_vp, _vp]),
     "cwgpu_plan_results": (ctypes.c_int, [_vp, _vp, _vp]),
     "cwgpu_plan_device_dist": (_vp, [_vp]),
+    "cwgpu_plan_cell_counts": (ctypes.c_int, [_vp, _vp]),
     "cwgpu_plan_destroy": (None, [_vp]),
     "cwgpu_synchronize": (ctypes.c_int, [_vp]),
 }
@@ -254,6 +255,12 @@ class Plan:
         st = np.zeros(max(self.npairs, 1), dtype=PAIR_STATS_DTYPE) if stats else None
         self.ctx._check(self._lib.cwgpu_plan_results(self._h, _ptr(dist), _ptr(st)), "cwgpu_plan_results")
         return (dist[: self.npairs], st[: self.npairs]) if stats else dist[: self.npairs]
+
+    def cell_counts(self):
+        """(forward, reverse, diff) cell updates of the last run, as the reference counts them."""
+        c = np.zeros(3, dtype=np.int64)
+        self.ctx._check(self._lib.cwgpu_plan_cell_counts(self._h, _ptr(c)), "cwgpu_plan_cell_counts")
+        return tuple(int(x) for x in c)
 
     def device_dist_ptr(self):
         return self._lib.cwgpu_plan_device_dist(self._h)

@@ -12,6 +12,13 @@ for the reference's FASTA fixtures with the shapes of the measured workloads:
 * DNA families: uniform ACGT root, substitution U(0.05, 0.4), indel 0.01 with
   geometric mean length 4.
 
+A Yule tree with N leaves is about 2 ln N branches deep, so applying those
+per-branch rates unchanged drives most pairs of a 1000-sequence family to
+background identity (~6%). To keep the 20-95% pairwise identity range the
+workloads are defined with, both rates of every branch are multiplied by
+min(1, depth / mean leaf depth), depth = 3 (protein) or 1.5 (DNA): the rates are per unit branch length
+and the tree is rescaled to a fixed expected depth.
+
 Sequences come out as ClustalW residue codes (index in
 "ABCDEFGHIKLMNOPQRSTUVWXYZ-", alignment/Sequence.cpp:63-83).
 """
@@ -32,19 +39,20 @@ PROTEIN_PROBS = _RR_FREQ / _RR_FREQ.sum()
 DNA_CODES = np.array([AMINO_ACID_CODES.index(c) for c in "ACGT"], dtype=np.int8)
 DNA_PROBS = np.full(4, 0.25)
 
-PROTEIN_MODEL = dict(codes=PROTEIN_CODES, probs=PROTEIN_PROBS, sub=(0.05, 0.3), indel=0.005, indel_mean=3.0)
-DNA_MODEL = dict(codes=DNA_CODES, probs=DNA_PROBS, sub=(0.05, 0.4), indel=0.01, indel_mean=4.0)
+# depth: the expected root-to-leaf branch count the rates are scaled to.
+PROTEIN_MODEL = dict(codes=PROTEIN_CODES, probs=PROTEIN_PROBS, sub=(0.05, 0.3), indel=0.005, indel_mean=3.0, depth=3.0)
+DNA_MODEL = dict(codes=DNA_CODES, probs=DNA_PROBS, sub=(0.05, 0.4), indel=0.01, indel_mean=4.0, depth=1.5)
 
 
-def _evolve(seq, rng, model, lo, hi):
+def _evolve(seq, rng, model, lo, hi, scale):
     codes, probs = model["codes"], model["probs"]
-    p_sub = rng.uniform(*model["sub"])
+    p_sub = rng.uniform(*model["sub"]) * scale
     out = seq.copy()
     mask = rng.random(len(out)) < p_sub
     n_sub = int(mask.sum())
     if n_sub:
         out[mask] = rng.choice(codes, size=n_sub, p=probs)
-    n_ev = rng.binomial(len(out), model["indel"])
+    n_ev = rng.binomial(len(out), model["indel"] * scale)
     if n_ev:
         pieces = list(out)
         for _ in range(n_ev):
@@ -71,12 +79,22 @@ def family(nseqs, root_len, seed, model=PROTEIN_MODEL):
     lo = max(1, int(np.floor(root_len * 0.9)))
     hi = max(lo, int(np.ceil(root_len * 1.1)))
     root = rng.choice(model["codes"], size=root_len, p=model["probs"]).astype(np.int8)
+    # Topology first (Yule process: a uniformly chosen leaf splits), then the
+    # depth-based rate scale, then the sequences top-down in split order.
+    splits = []
+    depth = [0]
+    for _ in range(max(0, nseqs - 1)):
+        i = int(rng.integers(len(depth)))
+        splits.append(i)
+        d = depth[i] + 1
+        depth[i] = d
+        depth.append(d)
+    scale = min(1.0, model["depth"] / max(1.0, float(np.mean(depth))))
     leaves = [root]
-    while len(leaves) < nseqs:
-        i = int(rng.integers(len(leaves)))
+    for i in splits:
         parent = leaves[i]
-        leaves[i] = _evolve(parent, rng, model, lo, hi)
-        leaves.append(_evolve(parent, rng, model, lo, hi))
+        leaves[i] = _evolve(parent, rng, model, lo, hi, scale)
+        leaves.append(_evolve(parent, rng, model, lo, hi, scale))
     perm = rng.permutation(len(leaves))
     return [leaves[k] for k in perm[:nseqs]]
 

@@ -42,16 +42,22 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     uint16_t* prof = prof_all + (size_t)warp * (kProfBytesPerWarp / sizeof(uint16_t));
     int2* bufA = g.scratch + (size_t)slot * 2 * (g.lmax + 1);
     int2* bufB = bufA + (g.lmax + 1);
+    unsigned long long acc[3] = {0, 0, 0};
     if (single >= 0) {
-        if (slot == 0) cwgpu::align_pair<kR>(g, single, prof, smat, bufA, bufB);
-        return;
+        if (slot == 0) cwgpu::align_pair<kR>(g, single, prof, smat, bufA, bufB, acc);
+    } else {
+        for (;;) {
+            unsigned long long k = 0;
+            if (lane == 0) k = atomicAdd(g.counter, 1ULL);
+            k = __shfl_sync(cwgpu::kFull, k, 0);
+            if (k >= (unsigned long long)g.npairs) break;
+            cwgpu::align_pair<kR>(g, (long long)g.order[k], prof, smat, bufA, bufB, acc);
+        }
     }
-    for (;;) {
-        unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(g.counter, 1ULL);
-        k = __shfl_sync(cwgpu::kFull, k, 0);
-        if (k >= (unsigned long long)g.npairs) break;
-        cwgpu::align_pair<kR>(g, (long long)g.order[k], prof, smat, bufA, bufB);
+    if (lane == 0 && g.cells && (acc[0] | acc[1] | acc[2])) {
+        atomicAdd(g.cells + 0, acc[0]);
+        atomicAdd(g.cells + 1, acc[1]);
+        atomicAdd(g.cells + 2, acc[2]);
     }
 }
 
@@ -78,7 +84,7 @@ struct cwgpu_context {
     int go_len = 0;
     int2* d_scratch = nullptr;
     size_t scratch_bytes = 0;
-    unsigned long long* d_counter = nullptr;
+    unsigned long long* d_counter = nullptr;  // [0] queue head, [1..3] cell counts
     int* d_err = nullptr;
     int grid = 0;
     bool derived_dirty = true;
@@ -197,6 +203,7 @@ cwgpu::PairArgs make_args(cwgpu_context* ctx, const int32_t* d_pairs, const int3
     g.stats = d_stats;
     g.scratch = ctx->d_scratch;
     g.counter = ctx->d_counter;
+    g.cells = ctx->d_counter + 1;
     g.err = ctx->d_err;
     g.npairs = npairs;
     g.lmax = ctx->lmax;
@@ -308,7 +315,8 @@ int cwgpu_create(int device, cwgpu_context** out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, 4 * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_matrix, sizeof(int32_t) * CWGPU_NUMRES * CWGPU_NUMRES);
@@ -435,7 +443,7 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
         e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaMemsetAsync(ctx->d_counter, 0, sizeof(unsigned long long), p->graph_stream);
+            cudaMemsetAsync(ctx->d_counter, 0, 4 * sizeof(unsigned long long), p->graph_stream);
             if (npairs > 0) {
                 const int grid = (int)std::min<int64_t>(ctx->grid, (npairs + kWarpsPerBlock - 1) / kWarpsPerBlock);
                 k_pairwise<<<grid, kWarpsPerBlock * 32, smem, p->graph_stream>>>(g, -1);
@@ -480,6 +488,17 @@ int cwgpu_plan_results(cwgpu_plan* p, float* dist_out, cwgpu_pair_stats* stats_o
 
 void* cwgpu_plan_device_dist(cwgpu_plan* p) { return p ? (void*)p->d_dist : nullptr; }
 
+int cwgpu_plan_cell_counts(cwgpu_plan* p, int64_t* counts) {
+    if (!p || !counts) return CWGPU_ERR_ARG;
+    cwgpu_context* ctx = p->ctx;
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    CW_CUDA(ctx, cudaDeviceSynchronize());
+    unsigned long long c[3];
+    CW_CUDA(ctx, cudaMemcpy(c, ctx->d_counter + 1, sizeof(c), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < 3; ++i) counts[i] = (int64_t)c[i];
+    return CWGPU_OK;
+}
+
 void cwgpu_plan_destroy(cwgpu_plan* p) {
     if (!p) return;
     if (p->ctx) cudaSetDevice(p->ctx->device);
@@ -521,6 +540,7 @@ int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t np
     if (e == cudaSuccess) e = cudaMalloc(&d_dist, sizeof(float) * npairs);
     if (e == cudaSuccess) e = cudaMalloc(&d_stats, sizeof(cwgpu_pair_stats) * npairs);
     if (e == cudaSuccess) e = cudaMemcpy(d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counter, 0, 4 * sizeof(unsigned long long), ctx->stream);
     if (e == cudaSuccess) {
         cwgpu::PairArgs g = make_args(ctx, d_pairs, nullptr, npairs, d_dist, d_stats);
         for (int64_t q = 0; q < npairs && e == cudaSuccess; ++q) {

@@ -228,6 +228,7 @@ struct PairArgs {
     int2* scratch;
     unsigned long long* counter;
     int* err;
+    unsigned long long* cells;  // [3]: forward, reverse (up to its break), diff
     long long npairs;
     int lmax;
     int ge;
@@ -244,7 +245,8 @@ struct PairArgs {
 template <int R>
 __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int go,
                          int ge, int gp1, int gp2, int2* bufA, int2* bufB, uint16_t* prof,
-                         const int* smat, int* err, int& mm_score, int& n_ident, int& n_match) {
+                         const int* smat, int* err, int& mm_score, int& n_ident, int& n_match,
+                         long long& cells) {
     const int lane = threadIdx.x & 31;
     constexpr int NMASK = (1 << 29) - 1;
     int stA = 0, stB = 0, stM = 0, stN = 0;
@@ -258,6 +260,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
     sp = 1;
     bool top = true;
     int ident = 0, matches = 0, mm = 0;
+    long long ncell = 0;  // diff() inner-loop iterations, counted as the reference runs them
 
     while (sp > 0) {
         --sp;
@@ -281,6 +284,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
                 continue;
             }
             // M == 1 (:443-477): best single column for residue A+1, first max.
+            ncell += N;
             int midh = -(tb + ge) - (te + ge * N);
             const int hh0 = -(te + ge) - (tb + ge * N);
             if (hh0 > midh) midh = hh0;
@@ -310,6 +314,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
 
         // Divide (:480-593): forward half on lanes 0-15, reverse half on 16-31.
         const int midi = M / 2;
+        ncell += (long long)M * N;
         Task t;
         if (lane < 16) {
             t.rseq = s1 + A;
@@ -430,12 +435,15 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
     mm_score = mm;
     n_ident = ident;
     n_match = matches;
+    cells = ncell;
 }
 
 // Aligns pair q: FullPairwiseAlign.cpp:112-183 for one (si, sj).
+// Adds the pair's algorithmic cell counts (the inner-loop iterations the
+// reference executes) to acc[0..2].
 template <int R>
 __device__ void align_pair(const PairArgs& g, long long q, uint16_t* prof, const int* smat, int2* bufA,
-                           int2* bufB) {
+                           int2* bufB, unsigned long long (&acc)[3]) {
     const int lane = threadIdx.x & 31;
     const int si = g.pairs[2 * q], sj = g.pairs[2 * q + 1];
     const int n = g.lens[si], m = g.lens[sj];
@@ -491,13 +499,21 @@ __device__ void align_pair(const PairArgs& g, long long q, uint16_t* prof, const
                 sb1 = se1 - (int)(rb.key >> 16);
                 sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
             }
+            // reversePass stops at the first cell reaching maxScore (:404-413).
+            if (rb.val >= max_score)
+                acc[1] += (unsigned long long)(se1 - sb1) * se2 + (unsigned long long)(se2 - sb2 + 1);
+            else
+                acc[1] += (unsigned long long)se1 * se2;
             __syncwarp();
         }
+        acc[0] += (unsigned long long)n * m;
 
         // diff + tracePath
         int mm = 0, ident = 0, matches = 0;
+        long long dcells = 0;
         mm_align<R>(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, g.gp1, g.gp2, bufA,
-                    bufB, prof, smat, g.err, mm, ident, matches);
+                    bufB, prof, smat, g.err, mm, ident, matches, dcells);
+        acc[2] += (unsigned long long)dcells;
 
         // distance (:170-181), float arithmetic with IEEE rounding.
         float mmv = (float)(100 * ident);

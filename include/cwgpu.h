@@ -156,6 +156,11 @@ int cwgpu_plan_launch(cwgpu_plan* plan, void* stream);
 int cwgpu_plan_results(cwgpu_plan* plan, float* dist_out, cwgpu_pair_stats* stats_out);
 /* Device address of the plan's float distance array (npairs entries). */
 void* cwgpu_plan_device_dist(cwgpu_plan* plan);
+/* Waits, then returns the algorithmic cell updates of the plan's last run:
+ * counts[0] forwardPass (n*m), counts[1] reversePass iterations up to its break
+ * (:351-414), counts[2] diff() inner-loop iterations (:450-566). These are the
+ * iteration counts the reference itself executes for the same pairs. */
+int cwgpu_plan_cell_counts(cwgpu_plan* plan, int64_t* counts);
 void cwgpu_plan_destroy(cwgpu_plan* plan);
 
 /* Waits for all work of the context and reports a kernel-side error flag. */

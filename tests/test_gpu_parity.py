@@ -88,3 +88,18 @@ def test_swapped_pair_order(ctx, oracle_mod):
     assert np.array_equal(dist, want["dist"])
     for f in STAT_FIELDS:
         assert np.array_equal(st[f], want[f]), f
+
+
+@pytest.mark.parametrize("name", ["synth_uneven_40", "fixture_100_97", "synth_long_6x3000", "edge_protein"])
+def test_cell_counts_match_oracle(ctx, oracle_mod, name):
+    """The kernel's algorithmic cell counters equal the reference's own
+    inner-loop iteration counts (forwardPass, reversePass up to its break, diff)."""
+    g = load_golden(name)
+    setup(ctx, g)
+    pairs = range_pairs(len(g["seqs"]), *g["range"])
+    plan = ctx.plan(pairs)
+    plan.launch()
+    fwd, rev, dif = plan.cell_counts()
+    plan.close()
+    want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    assert (fwd, rev, dif) == (int(want["cells_fwd"].sum()), int(want["cells_rev"].sum()), int(want["cells_diff"].sum()))
