@@ -14,7 +14,7 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcwgpu.so")
 
-SOURCES = ["cwgpu.cu"]
+SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu"]
 HEADERS = ["cwgpu_device.cuh"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 

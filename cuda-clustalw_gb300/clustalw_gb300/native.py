@@ -99,6 +99,10 @@ SIGNATURES = {
     "cwgpu_plan_cell_counts": (ctypes.c_int, [_vp, _vp]),
     "cwgpu_plan_destroy": (None, [_vp]),
     "cwgpu_synchronize": (ctypes.c_int, [_vp]),
+    "cwgpu_align_pairs_noalloc": (
+        ctypes.c_int,
+        [_vp, _vp, _vp, _i32, _i32, _vp, ctypes.POINTER(Params), _vp, _i64, _vp, _vp, _vp],
+    ),
 }
 
 _lib = None

@@ -163,6 +163,30 @@ void* cwgpu_plan_device_dist(cwgpu_plan* plan);
 int cwgpu_plan_cell_counts(cwgpu_plan* plan, int64_t* counts);
 void cwgpu_plan_destroy(cwgpu_plan* plan);
 
+/* ---- allocation-free variant ---------------------------------------------
+ * No counterpart in the reference. For callers that cannot call cudaMalloc:
+ * code inside a host framework that owns all device memory through its own
+ * pool, or a process whose device-memory budget is fixed at start-up. The
+ * caller passes device buffers it already owns; this call allocates nothing
+ * and uses one static device array of CWGPU_NOALLOC_SCRATCH_BYTES (16 MiB,
+ * held by every GPU that loads the library until the process exits) for all
+ * its working memory. Limit: sequences up to CWGPU_NOALLOC_MAX_LEN residues
+ * (longer max_len is rejected with CWGPU_ERR_ARG). All d_* pointers are device
+ * memory: codes/offsets/lens as for cwgpu_upload_seqs, d_matrix the 32x32
+ * int32 matrix, d_pairs 2*npairs int32, outputs d_dist (npairs floats) and
+ * d_stats (nullable). The first call on a device looks up the array's device
+ * address and should come before any stream capture. The call waits for its
+ * kernel on `stream` (a cudaStream_t, NULL = legacy default) and returns
+ * CWGPU_ERR_ARG if the device-side checks rejected an input (pair index,
+ * length above max_len, residue code outside [0, 31]). Calls share the array:
+ * calls whose GPU work overlaps race. */
+#define CWGPU_NOALLOC_MAX_LEN 8191
+#define CWGPU_NOALLOC_SCRATCH_BYTES (16u << 20)
+int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d_offsets, const int32_t* d_lens,
+                              int32_t nseqs, int32_t max_len, const int32_t* d_matrix,
+                              const cwgpu_params* params, const int32_t* d_pairs, int64_t npairs,
+                              float* d_dist, cwgpu_pair_stats* d_stats, void* stream);
+
 /* Waits for all work of the context and reports a kernel-side error flag. */
 int cwgpu_synchronize(cwgpu_context* ctx);
 
