@@ -71,6 +71,12 @@ PAIR_STATS_DTYPE = np.dtype(
     ]
 )
 
+class Tuning(ctypes.Structure):
+    """cwgpu_tuning: tiny-frame thresholds of the Myers-Miller stage."""
+
+    _fields_ = [("tiny_m", ctypes.c_int32), ("tiny_n", ctypes.c_int32)]
+
+
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
@@ -99,6 +105,8 @@ SIGNATURES = {
     "cwgpu_plan_cell_counts": (ctypes.c_int, [_vp, _vp]),
     "cwgpu_plan_destroy": (None, [_vp]),
     "cwgpu_synchronize": (ctypes.c_int, [_vp]),
+    "cwgpu_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
+    "cwgpu_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
     "cwgpu_align_pairs_noalloc": (
         ctypes.c_int,
         [_vp, _vp, _vp, _i32, _i32, _vp, ctypes.POINTER(Params), _vp, _i64, _vp, _vp, _vp],
@@ -234,6 +242,15 @@ class Context:
 
     def plan(self, pairs):
         return Plan(self, pairs)
+
+    def set_tuning(self, tiny_m, tiny_n):
+        t = Tuning(int(tiny_m), int(tiny_n))
+        self._check(self._lib.cwgpu_set_tuning(self._h, ctypes.byref(t)), "cwgpu_set_tuning")
+
+    def get_tuning(self):
+        t = Tuning()
+        self._check(self._lib.cwgpu_get_tuning(self._h, ctypes.byref(t)), "cwgpu_get_tuning")
+        return t.tiny_m, t.tiny_n
 
     def synchronize(self):
         self._check(self._lib.cwgpu_synchronize(self._h), "cwgpu_synchronize")

@@ -2,7 +2,8 @@
 // ordering, persistent graph-captured launch, plain one-launch-per-pair form.
 //
 // Device layout in HBM (all resident for the life of the context):
-//   codes   int8 residues, every sequence starting at a 16-byte boundary
+//   codes   int8 residues remapped to the K codes that occur, every sequence
+//           starting at a 16-byte boundary
 //   offs    int64 start of each sequence in `codes`
 //   lens    int32 sequence lengths n (getSeqLength)
 //   nres    int32 residues that are not gapPos1/gapPos2 (len1/len2 of :100-127)
@@ -26,32 +27,38 @@
 
 namespace {
 
-constexpr int kR = 4;             // rows per lane in the wavefront sweeps
-constexpr int kWarpsPerBlock = 4; // warps (= concurrent pairs) per CTA
-constexpr size_t kProfBytesPerWarp = 32 * 32 * kR * sizeof(uint16_t);
+constexpr int kWarpsPerBlock = 4;  // warps (= concurrent pairs) per CTA
 
 __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     k_pairwise(cwgpu::PairArgs g, long long single) {
     __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
-    extern __shared__ __align__(16) uint16_t prof_all[];
+    extern __shared__ __align__(16) uint16_t region_all[];
     for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = g.matrix[i];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int wpb = blockDim.x >> 5;
     const long long slot = (long long)blockIdx.x * wpb + warp;
-    uint16_t* prof = prof_all + (size_t)warp * (kProfBytesPerWarp / sizeof(uint16_t));
+    cwgpu::Env X;
+    X.smat = smat;
+    X.region = region_all + (size_t)warp * (cwgpu::warp_region_bytes(g.K) / sizeof(uint16_t));
+    X.K = g.K;
+    X.gp1 = g.gp1;
+    X.gp2 = g.gp2;
+    X.tiny_m = g.tiny_m;
+    X.tiny_n = g.tiny_n;
+    X.err = g.err;
     int2* bufA = g.scratch + (size_t)slot * 2 * (g.lmax + 1);
     int2* bufB = bufA + (g.lmax + 1);
     unsigned long long acc[3] = {0, 0, 0};
     if (single >= 0) {
-        if (slot == 0) cwgpu::align_pair<kR>(g, single, prof, smat, bufA, bufB, acc);
+        if (slot == 0) cwgpu::align_pair(g, single, X, bufA, bufB, acc);
     } else {
         for (;;) {
             unsigned long long k = 0;
             if (lane == 0) k = atomicAdd(g.counter, 1ULL);
             k = __shfl_sync(cwgpu::kFull, k, 0);
             if (k >= (unsigned long long)g.npairs) break;
-            cwgpu::align_pair<kR>(g, (long long)g.order[k], prof, smat, bufA, bufB, acc);
+            cwgpu::align_pair(g, (long long)g.order[k], X, bufA, bufB, acc);
         }
     }
     if (lane == 0 && g.cells && (acc[0] | acc[1] | acc[2])) {
@@ -74,7 +81,11 @@ struct cwgpu_context {
     int lmax = 0;
     std::vector<int32_t> lens;
     std::vector<int64_t> offs;
-    std::vector<int8_t> host_codes;  // for nres recomputation when params change
+    std::vector<int8_t> host_codes;  // original codes, for nres and the remap
+    int K = 0;                       // codes present in the sequences
+    int dense_of[CWGPU_NUMRES];      // original code -> dense index, -1 if absent
+    int code_of[CWGPU_NUMRES];       // dense index -> original code
+    int tiny_m = 32, tiny_n = 16;    // Myers-Miller frames solved one per lane
     int8_t* d_codes = nullptr;
     int64_t* d_offs = nullptr;
     int32_t* d_lens = nullptr;
@@ -87,6 +98,7 @@ struct cwgpu_context {
     unsigned long long* d_counter = nullptr;  // [0] queue head, [1..3] cell counts
     int* d_err = nullptr;
     int grid = 0;
+    int grid_K = -1;  // K the grid size was computed for
     bool derived_dirty = true;
     unsigned generation = 0;  // bumped whenever device inputs or scratch move
     std::string last_error;
@@ -156,6 +168,14 @@ int refresh_derived(cwgpu_context* ctx) {
     CW_CUDA(ctx, cudaMalloc(&ctx->d_go, sizeof(int32_t) * go.size()));
     CW_CUDA(ctx, cudaMemcpy(ctx->d_go, go.data(), sizeof(int32_t) * go.size(), cudaMemcpyHostToDevice));
     ctx->go_len = (int)go.size();
+    // Matrix over the dense codes, row stride 32 (entries past K unused).
+    if (ctx->has_matrix) {
+        std::vector<int32_t> dm(CWGPU_NUMRES * CWGPU_NUMRES, 0);
+        for (int a = 0; a < ctx->K; ++a)
+            for (int b = 0; b < ctx->K; ++b)
+                dm[a * CWGPU_NUMRES + b] = ctx->matrix[ctx->code_of[a] * CWGPU_NUMRES + ctx->code_of[b]];
+        CW_CUDA(ctx, cudaMemcpy(ctx->d_matrix, dm.data(), sizeof(int32_t) * dm.size(), cudaMemcpyHostToDevice));
+    }
     ctx->derived_dirty = false;
     ctx->generation++;
     return CWGPU_OK;
@@ -167,15 +187,21 @@ int gap_extend_of(const cwgpu_params& p) {
     return e;
 }
 
+size_t block_smem(int K, int warps) { return (size_t)cwgpu::warp_region_bytes(K) * warps; }
+
 // Persistent grid: as many CTAs as fit on every SM at once.
 int ensure_scratch(cwgpu_context* ctx) {
-    if (ctx->grid == 0) {
+    if (ctx->grid == 0 || ctx->grid_K != ctx->K) {
         int per_sm = 0;
-        const size_t smem = kProfBytesPerWarp * kWarpsPerBlock;
-        CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+        const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
+        CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                          (int)block_smem(CWGPU_NUMRES, kWarpsPerBlock)));
         CW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise, kWarpsPerBlock * 32, smem));
         if (per_sm < 1) per_sm = 1;
         ctx->grid = per_sm * ctx->sm_count;
+        ctx->grid_K = ctx->K;
+        ctx->scratch_bytes = 0;  // grid changed: resize below
+        dfree(ctx->d_scratch);
     }
     const size_t need = (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1) * sizeof(int2);
     if (need > ctx->scratch_bytes) {
@@ -208,8 +234,12 @@ cwgpu::PairArgs make_args(cwgpu_context* ctx, const int32_t* d_pairs, const int3
     g.npairs = npairs;
     g.lmax = ctx->lmax;
     g.ge = gap_extend_of(ctx->params);
-    g.gp1 = ctx->params.gap_pos1;
-    g.gp2 = ctx->params.gap_pos2;
+    const int gp1 = ctx->params.gap_pos1, gp2 = ctx->params.gap_pos2;
+    g.gp1 = (gp1 >= 0 && gp1 < CWGPU_NUMRES) ? ctx->dense_of[gp1] : -1;
+    g.gp2 = (gp2 >= 0 && gp2 < CWGPU_NUMRES) ? ctx->dense_of[gp2] : -1;
+    g.K = ctx->K;
+    g.tiny_m = ctx->tiny_m;
+    g.tiny_n = ctx->tiny_n;
     return g;
 }
 
@@ -353,8 +383,8 @@ int cwgpu_set_matrix(cwgpu_context* ctx, const int32_t* matrix) {
             return fail(ctx, CWGPU_ERR_MATRIX, "matrix entry outside the int16 profile range");
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
     memcpy(ctx->matrix, matrix, sizeof(ctx->matrix));
-    CW_CUDA(ctx, cudaMemcpy(ctx->d_matrix, matrix, sizeof(ctx->matrix), cudaMemcpyHostToDevice));
     ctx->has_matrix = true;
+    ctx->derived_dirty = true;  // the device copy is remapped to the dense codes
     ctx->generation++;
     return CWGPU_OK;
 }
@@ -389,6 +419,24 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     std::vector<int8_t> packed((size_t)std::max<int64_t>(total, 16), 0);
     for (int s = 0; s < nseqs; ++s)
         if (lens[s] > 0) memcpy(packed.data() + doffs[s], codes + offsets[s], lens[s]);
+    // Remap residue codes to the dense alphabet of the codes that occur, so the
+    // per-stripe score profile holds K rows instead of 32.
+    bool present[CWGPU_NUMRES] = {false};
+    for (int s = 0; s < nseqs; ++s)
+        for (int i = 0; i < lens[s]; ++i) present[codes[offsets[s] + i]] = true;
+    int K = 0, dense_of[CWGPU_NUMRES], code_of[CWGPU_NUMRES];
+    for (int c = 0; c < CWGPU_NUMRES; ++c) {
+        dense_of[c] = present[c] ? K : -1;
+        if (present[c]) code_of[K++] = c;
+    }
+    if (K == 0) {  // no residues at all: keep one code so launches stay well-formed
+        dense_of[0] = 0;
+        code_of[0] = 0;
+        K = 1;
+    }
+    std::vector<int8_t> dense(packed.size(), 0);
+    for (int s = 0; s < nseqs; ++s)
+        for (int i = 0; i < lens[s]; ++i) dense[doffs[s] + i] = (int8_t)dense_of[codes[offsets[s] + i]];
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
     dfree(ctx->d_codes);
     dfree(ctx->d_offs);
@@ -397,7 +445,7 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     CW_CUDA(ctx, cudaMalloc(&ctx->d_codes, packed.size()));
     CW_CUDA(ctx, cudaMalloc(&ctx->d_offs, sizeof(int64_t) * std::max(1, nseqs)));
     CW_CUDA(ctx, cudaMalloc(&ctx->d_lens, sizeof(int32_t) * std::max(1, nseqs)));
-    CW_CUDA(ctx, cudaMemcpy(ctx->d_codes, packed.data(), packed.size(), cudaMemcpyHostToDevice));
+    CW_CUDA(ctx, cudaMemcpy(ctx->d_codes, dense.data(), dense.size(), cudaMemcpyHostToDevice));
     if (nseqs) {
         CW_CUDA(ctx, cudaMemcpy(ctx->d_offs, doffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
         CW_CUDA(ctx, cudaMemcpy(ctx->d_lens, lens, sizeof(int32_t) * nseqs, cudaMemcpyHostToDevice));
@@ -407,6 +455,9 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     ctx->lens.assign(lens, lens + nseqs);
     ctx->offs = doffs;
     ctx->host_codes.swap(packed);
+    ctx->K = K;
+    memcpy(ctx->dense_of, dense_of, sizeof(dense_of));
+    memcpy(ctx->code_of, code_of, sizeof(code_of));
     ctx->has_seqs = true;
     ctx->derived_dirty = true;
     ctx->generation++;
@@ -439,7 +490,7 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
     if (e == cudaSuccess) {
         // Capture: reset the queue counter, then one persistent launch.
         cwgpu::PairArgs g = make_args(ctx, p->d_pairs, p->d_order, npairs, p->d_dist, p->d_stats);
-        const size_t smem = kProfBytesPerWarp * kWarpsPerBlock;
+        const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
         e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
@@ -544,7 +595,7 @@ int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t np
     if (e == cudaSuccess) {
         cwgpu::PairArgs g = make_args(ctx, d_pairs, nullptr, npairs, d_dist, d_stats);
         for (int64_t q = 0; q < npairs && e == cudaSuccess; ++q) {
-            k_pairwise<<<1, 32, kProfBytesPerWarp, ctx->stream>>>(g, (long long)q);
+            k_pairwise<<<1, 32, block_smem(ctx->K, 1), ctx->stream>>>(g, (long long)q);
             e = cudaGetLastError();
         }
     }
@@ -590,6 +641,23 @@ int cwgpu_pairwise_align(cwgpu_context* ctx, int32_t i_start, int32_t i_end, int
         const int64_t i = pairs[2 * q], j = pairs[2 * q + 1];
         elements[((j * (j + 1)) >> 1) + i] = (double)dist[q];
     }
+    return CWGPU_OK;
+}
+
+int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning) {
+    if (!ctx || !tuning) return CWGPU_ERR_ARG;
+    if (tuning->tiny_m < 0 || tuning->tiny_m > 256 || tuning->tiny_n < 0 || tuning->tiny_n > cwgpu::kTinyMaxN)
+        return fail(ctx, CWGPU_ERR_ARG, "tiny_m must be in [0, 256] and tiny_n in [0, 16]");
+    ctx->tiny_m = tuning->tiny_m;
+    ctx->tiny_n = tuning->tiny_n;
+    ctx->generation++;
+    return CWGPU_OK;
+}
+
+int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning) {
+    if (!ctx || !tuning) return CWGPU_ERR_ARG;
+    tuning->tiny_m = ctx->tiny_m;
+    tuning->tiny_n = ctx->tiny_n;
     return CWGPU_OK;
 }
 

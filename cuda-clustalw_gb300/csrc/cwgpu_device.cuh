@@ -9,15 +9,30 @@
 //   4. tracePath    (:231-278)  identity count, folded into diff's M==1 leaves
 //   5. distance     (:172-181)  float arithmetic identical to the reference
 //
-// All three dynamic-programming sweeps run on one primitive, `sweep`: a
-// row-striped anti-diagonal wavefront. Lane l of a W-lane segment owns R
-// consecutive rows of the current stripe and processes column c = t - l + 1
-// at step t; the H and E values of the row above arrive from lane l-1 by
-// __shfl_up_sync, the first lane reads them from the previous stripe's last
-// row (a global buffer, L2-resident) or from a closed-form boundary. Integer
-// recurrences use the DPX instructions (__viaddmax_s32, __vimax3_s32[_relu]).
-// Scores come from a per-stripe int16 profile in shared memory
-// (prof[code][lane][row]) so each step needs one conflict-free 8-byte load.
+// All dynamic-programming sweeps of steps 1-3 run on one primitive, `sweep`:
+// a row-striped anti-diagonal wavefront. Lane l of a W-lane segment owns R
+// consecutive rows of the current stripe and processes column c = t - l + 1 at
+// step t. H and E of the row above arrive from lane l-1 by __shfl_up_sync; the
+// segment's first lane takes them from the previous stripe's last row, which
+// the segment reads W columns at a time with one coalesced load and hands to
+// that lane by shuffle, or from the closed-form boundary of the first stripe.
+//
+// E and F are carried shifted by gapOpen+gapExtend (E' = E + goe, F' = F + goe)
+// so each cell costs five integer operations, three of them DPX:
+//   E'(r,c) = max(E'(r-1,c) - ge, H(r-1,c))                __viaddmax_s32
+//   F'(r,c) = max(F'(r,c-1) - ge, H(r,c-1))                __viaddmax_s32
+//   H(r,c)  = max(H(r-1,c-1) + s, max(E', F') - goe [, 0]) max + add + __viaddmax_s32[_relu]
+// which is the reference's recurrence written with fewer operations.
+//
+// Scores come from a per-stripe int16 profile in shared memory,
+// prof[code][lane][row], one conflict-free 16-byte load per step and lane.
+// Residues are remapped on the host to the K codes that occur (K <= 32), so
+// the profile holds K rows of codes.
+//
+// Myers-Miller frames small enough (M <= tiny_m, N <= tiny_n) are not swept
+// by the warp: they are queued, and 32 of them at a time are solved one per
+// lane with the reference's sequential loops, rows kept in the lane's column
+// of the warp's shared scratch.
 #pragma once
 
 #include <climits>
@@ -28,15 +43,25 @@
 namespace cwgpu {
 
 constexpr unsigned kFull = 0xffffffffu;
+constexpr int kR = 8;              // rows per lane in every sweep
+constexpr int kTinyMaxN = 16;      // tiny frames: N <= kTinyMaxN (shared-memory rows)
+constexpr int kTinyStride = kTinyMaxN + 1;
+constexpr int kTinyWords = 4 * kTinyStride * 32;  // HH, DD, RR, SS for 32 lanes
+constexpr int kTinyStack = 16;
+
+// Bytes of the per-warp shared region: the stripe profile or the tiny-frame rows.
+__host__ __device__ constexpr int warp_region_bytes(int K) {
+    return (K * 32 * kR * 2 > kTinyWords * 4) ? K * 32 * kR * 2 : kTinyWords * 4;
+}
 
 // One rectangular sweep. Row r (0-based) uses residue rseq[r * rdir]; column c
-// (1-based) uses residue cseq[(c - 1) * cdir]. Boundaries (closed form, which
-// is what every sweep of the reference uses):
+// (1-based) uses residue cseq[(c - 1) * cdir]. Closed-form boundaries, which
+// is what every sweep of the reference uses:
 //   H(-1, c) = ht0 - c*hts        E(-1, c) = H(-1, c) - eo      (c >= 1)
 //   H(r, 0)  = hl0 - (r+1)*hls    F(r, 0)  = H(r, 0) - fo
 //   H(-1, 0) = 0
-// For stripes after the first, H/E of the row above come from buf[c]. In
-// MODE_GLOBAL the last row's H/E are left in buf[1..cols].
+// buf[c] (c = 1..cols) carries (H, E') of the last row of a stripe to the next
+// stripe, and in MODE_GLOBAL holds the final row on return.
 struct Task {
     const int8_t* rseq;
     const int8_t* cseq;
@@ -54,54 +79,171 @@ struct Best {
     unsigned key;  // (row << 16) | col of the winning cell
 };
 
-template <int R>
-__device__ __forceinline__ void unpack_scores(uint2 w, int (&s)[R]);
+// Per-block constants the device functions read.
+struct Env {
+    const int* smat;     // shared 32x32 matrix over remapped codes
+    uint16_t* region;    // this warp's shared region (profile or tiny rows)
+    int K;               // number of remapped codes
+    int gp1, gp2;        // remapped gapPos1 / gapPos2 (-1 if absent)
+    int tiny_m, tiny_n;  // tiny-frame thresholds
+    int* err;
+};
 
-template <>
-__device__ __forceinline__ void unpack_scores<4>(uint2 w, int (&s)[4]) {
+template <int R>
+struct SweepState {
+    int hl[R];  // H(r, c-1)
+    int fp[R];  // F'(r, c-1)
+    int rm[R];  // tracked maximum per row
+    int rc[R];  // its first column
+    int diag;   // H of the row above the lane's first row, column c-1
+    int hout, eout, thr, bnext;
+    int ch, ce, nh, ne;  // boundary chunks: current and next W columns
+};
+
+__device__ __forceinline__ void unpack8(uint4 w, int (&s)[8]) {
     s[0] = (int)(int16_t)(w.x & 0xffffu);
     s[1] = ((int)w.x) >> 16;
     s[2] = (int)(int16_t)(w.y & 0xffffu);
     s[3] = ((int)w.y) >> 16;
+    s[4] = (int)(int16_t)(w.z & 0xffffu);
+    s[5] = ((int)w.z) >> 16;
+    s[6] = (int)(int16_t)(w.w & 0xffffu);
+    s[7] = ((int)w.w) >> 16;
 }
 
-// Fills this lane's slice of the stripe profile: prof[(b*32 + lane)*R + k] =
-// matrix[a[k]][b] for all 32 codes b. Lane l starts at code l so the reads of
-// the shared matrix hit 32 different banks.
-template <int R>
-__device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, const int (&a)[R],
-                                              int lane) {
-    static_assert(R == 4, "profile packing written for R == 4");
-#pragma unroll 4
-    for (int i = 0; i < 32; ++i) {
-        const int b = (i + lane) & 31;
-        const unsigned v0 = (unsigned)smat[a[0] * 32 + b] & 0xffffu;
-        const unsigned v1 = (unsigned)smat[a[1] * 32 + b] & 0xffffu;
-        const unsigned v2 = (unsigned)smat[a[2] * 32 + b] & 0xffffu;
-        const unsigned v3 = (unsigned)smat[a[3] * 32 + b] & 0xffffu;
-        *reinterpret_cast<uint2*>(prof + (b * 32 + lane) * R) = make_uint2(v0 | (v1 << 16), v2 | (v3 << 16));
+__device__ __forceinline__ unsigned pack2(int lo, int hi) {
+    return ((unsigned)lo & 0xffffu) | ((unsigned)hi << 16);
+}
+
+// prof[(b*32 + lane)*8 + k] = matrix[a[k]][b] for the K codes b. Lane l starts
+// at code l % K so that its shared-matrix reads spread over the banks.
+__device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, const int (&a)[8], int lane,
+                                              int K) {
+    int b = lane % K;
+    for (int i = 0; i < K; ++i) {
+        uint4 w;
+        w.x = pack2(smat[a[0] * 32 + b], smat[a[1] * 32 + b]);
+        w.y = pack2(smat[a[2] * 32 + b], smat[a[3] * 32 + b]);
+        w.z = pack2(smat[a[4] * 32 + b], smat[a[5] * 32 + b]);
+        w.w = pack2(smat[a[6] * 32 + b], smat[a[7] * 32 + b]);
+        *reinterpret_cast<uint4*>(prof + (b * 32 + lane) * 8) = w;
+        b = (b + 1 == K) ? 0 : b + 1;
+    }
+}
+
+// The steps of one stripe. Lane 0 of the segment takes the row above from
+// the chunk registers (W columns per lane-wide load: the previous stripe's last
+// row, or the closed-form top boundary for the first stripe). PARTIAL: some
+// rows of the stripe are past the task's last row; they pass the row above
+// through so the segment's last used lane still emits the last real row. One
+// loop body per (MODE, PARTIAL) keeps the hot code small enough for the
+// instruction cache; lanes outside their column range skip the body.
+template <int R, int W, int MODE, bool PARTIAL>
+__device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T, SweepState<R>& S, int sl,
+                                           int nvalid, bool writer, int ge, int goe, int thresh,
+                                           const uint16_t* prof_lane) {
+    const int cmax = T.cols - 1;
+    for (int t = 0; t < nsteps; ++t) {
+        const int c = t - sl + 1;
+        int hin = __shfl_up_sync(kFull, S.hout, 1, W);
+        int ein = __shfl_up_sync(kFull, S.eout, 1, W);
+        const int idx = t & (W - 1);
+        const int bh = __shfl_sync(kFull, S.ch, idx, W);
+        const int be = __shfl_sync(kFull, S.ce, idx, W);
+        if (sl == 0) {
+            hin = bh;
+            ein = be;
+        }
+        if (idx == W - 1) {
+            S.ch = S.nh;
+            S.ce = S.ne;
+            const int col = (t / W + 2) * W + 1 + sl;
+            if (first) {
+                S.nh = T.ht0 - col * T.hts;
+                S.ne = S.nh - T.eo + goe;
+            } else if (col <= T.cols) {
+                const int2 v = T.buf[col];
+                S.nh = v.x;
+                S.ne = v.y;
+            }
+        }
+        const int b = S.bnext;
+        S.bnext = (int)__ldg(T.cseq + min(max(c, 0), cmax) * T.cdir);  // next step's column, clamped in range
+        if ((unsigned)(c - 1) < (unsigned)T.cols) {
+            int sc[R];
+            unpack8(*reinterpret_cast<const uint4*>(prof_lane + b * (32 * R)), sc);
+            int hup = hin, eup = ein, d = S.diag;
+            int hs[R];
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                int e = __viaddmax_s32(eup, -ge, hup);
+                const int f = __viaddmax_s32(S.fp[k], -ge, S.hl[k]);
+                const int mx = max(e, f);
+                int h;
+                if (MODE == MODE_LOCAL_FWD)
+                    h = __viaddmax_s32_relu(mx, -goe, d + sc[k]);
+                else
+                    h = __viaddmax_s32(mx, -goe, d + sc[k]);
+                if (PARTIAL) {
+                    const bool v = k < nvalid;
+                    h = v ? h : hup;
+                    e = v ? e : eup;
+                }
+                d = S.hl[k];
+                S.hl[k] = h;
+                S.fp[k] = f;
+                hup = h;
+                eup = e;
+                hs[k] = h;
+            }
+            S.hout = hup;
+            S.eout = eup;
+            S.diag = hin;
+            if (MODE != MODE_GLOBAL) {
+                int sm = hs[0];
+#pragma unroll
+                for (int k = 1; k + 1 < R; k += 2) sm = __vimax3_s32(sm, hs[k], hs[k + 1]);
+                if ((R & 1) == 0) sm = max(sm, hs[R - 1]);
+                if (MODE == MODE_LOCAL_REV) sm = min(sm, thresh);
+                if (sm >= S.thr) {
+#pragma unroll
+                    for (int k = 0; k < R; ++k) {
+                        const int hv = (MODE == MODE_LOCAL_REV) ? min(hs[k], thresh) : hs[k];
+                        if (hv > S.rm[k]) {
+                            S.rm[k] = hv;
+                            S.rc[k] = c;
+                        }
+                    }
+                    S.thr = sm;
+                }
+            }
+            if (writer) T.buf[c] = make_int2(hup, eup);
+        }
     }
 }
 
 // The wavefront sweep. W = lanes per segment (32: one task per warp, 16: two
-// tasks, one per half-warp). MODE_LOCAL_FWD tracks the first maximum in
-// row-major order (forwardPass's strict `hh > maxScore`); MODE_LOCAL_REV
-// tracks the first cell, in the sweep's own order, of the running maximum of
-// min(H, thresh) (reversePass's strict `hh > cost` with its break at
-// cost >= maxScore) and stops after the first stripe that reached thresh.
+// tasks, one per half-warp; the two tasks have the same column count).
+// MODE_LOCAL_FWD tracks the first maximum in row-major order (forwardPass's
+// strict `hh > maxScore`); MODE_LOCAL_REV tracks the first cell, in the sweep's
+// row-major order, of the maximum of min(H, thresh) (reversePass's strict
+// `hh > cost` and its break at cost >= maxScore) and stops after the first
+// stripe that reached thresh. Tracking runs on the per-step maximum of the
+// lane's rows; only when it reaches the lane's running maximum are the rows
+// examined one by one.
 template <int R, int W, int MODE>
-__device__ void sweep(const Task& T, int go, int ge, int thresh, uint16_t* prof, const int* smat,
-                      Best& best) {
+__device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, Best& best) {
+    static_assert(R == 8, "profile layout written for R == 8");
     const int lane = threadIdx.x & 31;
     const int sl = lane & (W - 1);
     const int goe = go + ge;
     constexpr int RPS = W * R;
     const int nstr = T.rows > 0 ? (T.rows + RPS - 1) / RPS : 0;
     const int nstr_max = __reduce_max_sync(kFull, nstr);
-    const bool use_prof = T.cols >= 24;
-    const bool use_prof_w = __all_sync(kFull, use_prof);
+    const uint16_t* prof_lane = X.region + lane * R;
     best.val = 0;
     best.key = 0xffffffffu;
+    SweepState<R> S;
 
     for (int s = 0; s < nstr_max; ++s) {
         const int srow0 = s * RPS;
@@ -113,93 +255,61 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, uint16_t* prof,
         const int nsteps_max = __reduce_max_sync(kFull, nsteps);
         const bool last = (s == nstr - 1);
         const bool writer = (sl == lused - 1) && (MODE == MODE_GLOBAL || !last);
+        const bool full = __all_sync(kFull, seg_rows == RPS);
 
         int a[R];
 #pragma unroll
         for (int k = 0; k < R; ++k) a[k] = (k < nvalid) ? (int)__ldg(T.rseq + (lrow0 + k) * T.rdir) : 0;
-        if (use_prof_w) build_profile<R>(prof, smat, a, lane);
-        __syncwarp();  // previous stripe's buf writes are visible to the first lane
+        __syncwarp();  // previous users of the shared region are done
+        build_profile(X.region, X.smat, a, lane, X.K);
+        __syncwarp();  // previous stripe's buf writes visible to the whole segment
 
-        int hl[R], f[R], rm[R], rc[R];
+        const int gbest = best.val;
 #pragma unroll
         for (int k = 0; k < R; ++k) {
-            hl[k] = T.hl0 - (lrow0 + k + 1) * T.hls;
-            f[k] = hl[k] - T.fo;
-            rm[k] = 0;
-            rc[k] = 0;
+            S.hl[k] = T.hl0 - (lrow0 + k + 1) * T.hls;
+            S.fp[k] = S.hl[k] - T.fo + goe;
+            S.rm[k] = gbest;
+            S.rc[k] = 0;
         }
-        int diag = (lrow0 == 0) ? 0 : T.hl0 - lrow0 * T.hls;
-        int hout = 0, eout = 0;
-
-        for (int t = 0; t < nsteps_max; ++t) {
-            const int c = t - sl + 1;
-            int hin = __shfl_up_sync(kFull, hout, 1, W);
-            int ein = __shfl_up_sync(kFull, eout, 1, W);
-            if (c >= 1 && c <= T.cols && nvalid > 0) {
-                if (sl == 0) {
-                    if (s == 0) {
-                        hin = T.ht0 - c * T.hts;
-                        ein = hin - T.eo;
-                    } else {
-                        const int2 v = T.buf[c];
-                        hin = v.x;
-                        ein = v.y;
-                    }
-                }
-                const int b = (int)__ldg(T.cseq + (c - 1) * T.cdir);
-                int sc[R];
-                if (use_prof_w) {
-                    const uint2 w = *reinterpret_cast<const uint2*>(prof + (b * 32 + lane) * R);
-                    unpack_scores<R>(w, sc);
-                } else {
-#pragma unroll
-                    for (int k = 0; k < R; ++k) sc[k] = smat[a[k] * 32 + b];
-                }
-                int hup = hin, eup = ein, d = diag;
-#pragma unroll
-                for (int k = 0; k < R; ++k) {
-                    if (k < nvalid) {
-                        const int e = __viaddmax_s32(eup, -ge, hup - goe);
-                        f[k] = __viaddmax_s32(f[k], -ge, hl[k] - goe);
-                        int h;
-                        if (MODE == MODE_LOCAL_FWD)
-                            h = __vimax3_s32_relu(d + sc[k], e, f[k]);
-                        else
-                            h = __vimax3_s32(d + sc[k], e, f[k]);
-                        d = hl[k];
-                        hl[k] = h;
-                        hup = h;
-                        eup = e;
-                        if (MODE == MODE_LOCAL_FWD) {
-                            if (h > rm[k]) {
-                                rm[k] = h;
-                                rc[k] = c;
-                            }
-                        } else if (MODE == MODE_LOCAL_REV) {
-                            const int hc = min(h, thresh);
-                            if (hc > rm[k]) {
-                                rm[k] = hc;
-                                rc[k] = c;
-                            }
-                        }
-                    }
-                }
-                hout = hup;
-                eout = eup;
-                diag = hin;
-                if (writer) T.buf[c] = make_int2(hout, eout);
+        S.diag = (lrow0 == 0) ? 0 : T.hl0 - lrow0 * T.hls;
+        S.hout = 0;
+        S.eout = 0;
+        S.thr = gbest + 1;
+        S.bnext = (int)__ldg(T.cseq);  // column 1, used by lane 0 at step 0
+        const bool first = (s == 0);
+        if (first) {
+            S.ch = T.ht0 - (1 + sl) * T.hts;
+            S.ce = S.ch - T.eo + goe;
+            S.nh = T.ht0 - (W + 1 + sl) * T.hts;
+            S.ne = S.nh - T.eo + goe;
+        } else {
+            S.ch = S.ce = S.nh = S.ne = 0;
+            if (1 + sl <= T.cols) {
+                const int2 v = T.buf[1 + sl];
+                S.ch = v.x;
+                S.ce = v.y;
+            }
+            if (W + 1 + sl <= T.cols) {
+                const int2 v = T.buf[W + 1 + sl];
+                S.nh = v.x;
+                S.ne = v.y;
             }
         }
+        if (full)
+            run_stripe<R, W, MODE, false>(nsteps_max, first, T, S, sl, nvalid, writer, ge, goe, thresh, prof_lane);
+        else
+            run_stripe<R, W, MODE, true>(nsteps_max, first, T, S, sl, nvalid, writer, ge, goe, thresh, prof_lane);
 
         if (MODE != MODE_GLOBAL) {
-            // Earliest row of this lane with the lane's maximum (rows ascend with k).
-            int lv = 0;
+            // Earliest row of this lane holding the lane's maximum (rows ascend with k).
+            int lv = gbest;
             unsigned lk = 0xffffffffu;
 #pragma unroll
             for (int k = 0; k < R; ++k) {
-                if (k < nvalid && rm[k] > lv) {
-                    lv = rm[k];
-                    lk = ((unsigned)(lrow0 + k) << 16) | (unsigned)rc[k];
+                if (k < nvalid && S.rm[k] > lv) {
+                    lv = S.rm[k];
+                    lk = ((unsigned)(lrow0 + k) << 16) | (unsigned)S.rc[k];
                 }
             }
             const int wv = __reduce_max_sync(kFull, lv);
@@ -210,59 +320,203 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, uint16_t* prof,
             }
             if (MODE == MODE_LOCAL_REV && best.val >= thresh) break;
         }
-        __syncwarp();
     }
+    __syncwarp();
 }
 
-struct PairArgs {
-    const int8_t* codes;
-    const int64_t* offs;
-    const int32_t* lens;
-    const int32_t* nres;
-    const int32_t* pairs;
-    const int32_t* order;
-    const int32_t* go_table;
-    const int32_t* matrix;
-    float* dist;
-    cwgpu_pair_stats* stats;
-    int2* scratch;
-    unsigned long long* counter;
-    int* err;
-    unsigned long long* cells;  // [3]: forward, reverse (up to its break), diff
-    long long npairs;
-    int lmax;
-    int ge;
-    int gp1, gp2;
-};
+// ---------------------------------------------------------------- tiny frames
 
-// Myers-Miller recursion (FullPairwiseAlign.cpp:418-612) on an explicit stack
-// held in registers (lane k holds frame k). Frames are independent once their
-// (A, B, M, N, tb, te) are known, and the identity count and match count are
-// sums over the M == 1 leaves, so the traversal order is free; the top frame's
-// score is diff()'s return value. tb/te are always 0 or gapOpen, kept as flags.
-// s1/s2 are 0-based code pointers: the reference's 1-based residue seq1[A + i]
-// is s1[A + i - 1].
-template <int R>
-__device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int go,
-                         int ge, int gp1, int gp2, int2* bufA, int2* bufB, uint16_t* prof,
-                         const int* smat, int* err, int& mm_score, int& n_ident, int& n_match,
+// Sequential Myers-Miller (FullPairwiseAlign.cpp:418-612) on one lane for one
+// frame and its whole subtree. Rows live in this lane's column of the warp's
+// shared scratch (word j*32 + lane, conflict-free), the frame stack in local
+// memory. Returns the frame's score; adds identities, matches and diff()
+// inner-loop iterations.
+static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int tbf0, int tef0, int go,
+                       int ge, const Env& X, int* scratch, int& ident, int& matches, long long& cells) {
+    const int lane = threadIdx.x & 31;
+    int* HH = scratch + lane;
+    int* DD = HH + kTinyStride * 32;
+    int* RR = DD + kTinyStride * 32;
+    int* SS = RR + kTinyStride * 32;
+#define TI(arr, j) arr[(j) * 32]
+    int4 stk[kTinyStack];
+    int sp = 0;
+    stk[sp++] = make_int4(A0, B0, M0, N0 | (tbf0 << 29) | (tef0 << 30));
+    int root_score = 0;
+    bool root = true;
+    while (sp > 0) {
+        const int4 fr = stk[--sp];
+        const int A = fr.x, B = fr.y, M = fr.z;
+        const int N = fr.w & ((1 << 29) - 1);
+        const int tbf = (fr.w >> 29) & 1, tef = (fr.w >> 30) & 1;
+        const int tb = tbf ? go : 0, te = tef ? go : 0;
+        int midh;
+        if (N <= 0) {
+            midh = -(M > 0 ? tb + ge * M : 0);
+        } else if (M <= 1) {
+            if (M <= 0) {
+                midh = -(tb + ge * N);
+            } else {
+                cells += N;
+                midh = -(tb + ge) - (te + ge * N);
+                const int hh0 = -(te + ge) - (tb + ge * N);
+                if (hh0 > midh) midh = hh0;
+                int midj = 0;
+                const int* row = X.smat + 32 * (int)__ldg(s1 + A);
+                for (int j = 1; j <= N; ++j) {
+                    const int hh = row[__ldg(s2 + B + j - 1)] - (N - j > 0 ? te + ge * (N - j) : 0) -
+                                   (j - 1 > 0 ? tb + ge * (j - 1) : 0);
+                    if (hh > midh) {
+                        midh = hh;
+                        midj = j;
+                    }
+                }
+                if (midj > 0) {
+                    ++matches;
+                    const int ra = __ldg(s1 + A), rb = __ldg(s2 + B + midj - 1);
+                    if (ra != X.gp1 && rb != X.gp2 && ra == rb) ++ident;
+                }
+            }
+        } else {
+            cells += (long long)M * N;
+            const int midi = M / 2;
+            int t = -tb;
+            TI(HH, 0) = 0;
+            for (int j = 1; j <= N; ++j) {
+                t -= ge;
+                TI(HH, j) = t;
+                TI(DD, j) = t - go;
+            }
+            t = -tb;
+            for (int i = 1; i <= midi; ++i) {
+                const int* row = X.smat + 32 * (int)__ldg(s1 + A + i - 1);
+                int s = TI(HH, 0);
+                int hh = t = t - ge;
+                TI(HH, 0) = hh;
+                int f = t - go;
+                for (int j = 1; j <= N; ++j) {
+                    f = max(f - ge, hh - go - ge);
+                    const int e = max(TI(DD, j) - ge, TI(HH, j) - go - ge);
+                    hh = max(max(s + row[__ldg(s2 + B + j - 1)], f), e);
+                    s = TI(HH, j);
+                    TI(HH, j) = hh;
+                    TI(DD, j) = e;
+                }
+            }
+            TI(DD, 0) = TI(HH, 0);
+            TI(RR, N) = 0;
+            t = -te;
+            for (int j = N - 1; j >= 0; --j) {
+                t -= ge;
+                TI(RR, j) = t;
+                TI(SS, j) = t - go;
+            }
+            t = -te;
+            for (int i = M - 1; i >= midi; --i) {
+                const int* row = X.smat + 32 * (int)__ldg(s1 + A + i);
+                int s = TI(RR, N);
+                int hh = t = t - ge;
+                TI(RR, N) = hh;
+                int f = t - go;
+                for (int j = N - 1; j >= 0; --j) {
+                    f = max(f - ge, hh - go - ge);
+                    const int e = max(TI(SS, j) - ge, TI(RR, j) - go - ge);
+                    hh = max(max(s + row[__ldg(s2 + B + j)], f), e);
+                    s = TI(RR, j);
+                    TI(RR, j) = hh;
+                    TI(SS, j) = e;
+                }
+            }
+            TI(SS, N) = TI(RR, N);
+            midh = TI(HH, 0) + TI(RR, 0);
+            int midj = 0;
+            bool type2 = false;
+            for (int j = 0; j <= N; ++j) {
+                const int hh = TI(HH, j) + TI(RR, j);
+                if (hh >= midh)
+                    if (hh > midh || (TI(HH, j) != TI(DD, j) && TI(RR, j) == TI(SS, j))) {
+                        midh = hh;
+                        midj = j;
+                    }
+            }
+            for (int j = N; j >= 0; --j) {
+                const int hh = TI(DD, j) + TI(SS, j) + go;
+                if (hh > midh) {
+                    midh = hh;
+                    midj = j;
+                    type2 = true;
+                }
+            }
+            if (sp + 2 > kTinyStack) {
+                atomicExch(X.err, 1);
+                break;
+            }
+            if (!type2) {
+                stk[sp++] = make_int4(A + midi, B + midj, M - midi, (N - midj) | (1 << 29) | (tef << 30));
+                stk[sp++] = make_int4(A, B, midi, midj | (tbf << 29) | (1 << 30));
+            } else {
+                stk[sp++] = make_int4(A + midi + 1, B + midj, M - midi - 1, (N - midj) | (tef << 30));
+                stk[sp++] = make_int4(A, B, midi - 1, midj | (tbf << 29));
+            }
+        }
+        if (root) root_score = midh;
+        root = false;
+    }
+#undef TI
+    return root_score;
+}
+
+// ---------------------------------------------------------------- diff()
+
+// Myers-Miller recursion (FullPairwiseAlign.cpp:418-612) for one pair. Large
+// frames are divided by the warp: forward half on lanes 0-15 and reverse half
+// on lanes 16-31, then the midpoint scans as warp reductions. Frames go on an
+// explicit stack held in registers (lane k holds frame k); tiny frames go on a
+// queue (lane k holds entry k) that is solved 32 at a time by lane_mm. Frames
+// are independent once (A, B, M, N, tb, te) are known, and the identity and
+// match counts are sums over the M == 1 leaves, so the traversal order is
+// free; the top frame's score is diff()'s return value. tb/te are always 0 or
+// gapOpen, kept as flags. s1/s2 are 0-based: the reference's 1-based residue
+// seq1[A + i] is s1[A + i - 1].
+static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int go, int ge,
+                         int2* bufA, int2* bufB, const Env& X, int& mm_score, int& n_ident, int& n_match,
                          long long& cells) {
     const int lane = threadIdx.x & 31;
     constexpr int NMASK = (1 << 29) - 1;
-    int stA = 0, stB = 0, stM = 0, stN = 0;
-    int sp = 0;
+    const int goe = go + ge;
+    int stA = 0, stB = 0, stM = 0, stN = 0;  // stack entry `lane`
+    int qA = 0, qB = 0, qM = 0, qN = 0;      // tiny-queue entry `lane`
     if (lane == 0) {
         stA = A0;
         stB = B0;
         stM = M0;
         stN = N0 & NMASK;
     }
-    sp = 1;
+    int sp = 1, nq = 0;
     bool top = true;
     int ident = 0, matches = 0, mm = 0;
-    long long ncell = 0;  // diff() inner-loop iterations, counted as the reference runs them
+    long long ncell = 0;
+    bool q_has_top = false;  // queue entry 0 is the top frame
 
-    while (sp > 0) {
+    while (sp > 0 || nq > 0) {
+        if (sp == 0 || nq == 32) {
+            // Solve the queued tiny frames, one per lane.
+            __syncwarp();
+            int li = 0, lm = 0, score = 0;
+            long long lc = 0;
+            if (lane < nq) {
+                score = lane_mm(s1, s2, qA, qB, qM, qN & NMASK, (qN >> 29) & 1, (qN >> 30) & 1, go, ge, X,
+                                reinterpret_cast<int*>(X.region), li, lm, lc);
+            }
+            __syncwarp();
+            ident += __reduce_add_sync(kFull, li);
+            matches += __reduce_add_sync(kFull, lm);
+            ncell += (long long)__reduce_add_sync(kFull, (unsigned)lc);
+            if (q_has_top) mm = __shfl_sync(kFull, score, 0);
+            q_has_top = false;
+            nq = 0;
+            continue;
+        }
         --sp;
         const int A = __shfl_sync(kFull, stA, sp);
         const int B = __shfl_sync(kFull, stB, sp);
@@ -272,6 +526,18 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
         const int tbf = (NN >> 29) & 1, tef = (NN >> 30) & 1;
         const int tb = tbf ? go : 0, te = tef ? go : 0;
 
+        if (M <= X.tiny_m && N <= X.tiny_n) {
+            if (lane == nq) {
+                qA = A;
+                qB = B;
+                qM = M;
+                qN = NN;
+            }
+            if (top) q_has_top = true;  // only possible as entry 0
+            top = false;
+            ++nq;
+            continue;
+        }
         if (N <= 0) {  // del(M); return -tbgap(M, tb)
             if (top) mm = -(M > 0 ? tb + ge * M : 0);
             top = false;
@@ -283,7 +549,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
                 top = false;
                 continue;
             }
-            // M == 1 (:443-477): best single column for residue A+1, first max.
+            // M == 1 with a long row (:443-477): best single column, first max.
             ncell += N;
             int midh = -(tb + ge) - (te + ge * N);
             const int hh0 = -(te + ge) - (tb + ge * N);
@@ -292,7 +558,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
             int bv = INT_MIN, bj = 0x7fffffff;
             for (int j = lane + 1; j <= N; j += 32) {
                 const int rb = (int)__ldg(s2 + B + j - 1);
-                const int v = smat[ra * 32 + rb] - (N - j > 0 ? te + ge * (N - j) : 0) -
+                const int v = X.smat[ra * 32 + rb] - (N - j > 0 ? te + ge * (N - j) : 0) -
                               (j - 1 > 0 ? tb + ge * (j - 1) : 0);
                 if (v > bv) {
                     bv = v;
@@ -305,7 +571,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
                 midh = wv;
                 const int rb = (int)__ldg(s2 + B + wj - 1);
                 ++matches;
-                if (ra != gp1 && rb != gp2 && ra == rb) ++ident;
+                if (ra != X.gp1 && rb != X.gp2 && ra == rb) ++ident;
             }
             if (top) mm = midh;
             top = false;
@@ -341,15 +607,14 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
         t.hls = ge;
         t.fo = go;
         Best unused;
-        sweep<R, 16, MODE_GLOBAL>(t, go, ge, 0, prof, smat, unused);
-        __syncwarp();
+        sweep<kR, 16, MODE_GLOBAL>(t, go, ge, 0, X, unused);
 
         // Midpoint scans (:570-593). Scan 1 keeps the first j reaching the
         // maximum of HH+RR, replaced by the last tied j with HH!=DD && RR==SS;
         // scan 2 switches to a type-2 midpoint at the largest j whose
-        // DD+SS+gapOpen is strictly above that maximum.
-        const int HH0 = -tb - midi * ge;       // HH[0] = DD[0]
-        const int RRN = -te - (M - midi) * ge; // RR[N] = SS[N]
+        // DD+SS+gapOpen is strictly above that maximum. buf holds E' = E+goe.
+        const int HH0 = -tb - midi * ge;        // HH[0] = DD[0]
+        const int RRN = -te - (M - midi) * ge;  // RR[N] = SS[N]
         int b1 = INT_MIN, j1 = 0x7fffffff, jc = -1, b2 = INT_MIN, j2 = -1;
         for (int j = lane; j <= N; j += 32) {
             int hh, dd, rr, ss;
@@ -358,14 +623,14 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
             } else {
                 const int2 v = bufA[j];
                 hh = v.x;
-                dd = v.y;
+                dd = v.y - goe;
             }
             if (j == N) {
                 rr = ss = RRN;
             } else {
                 const int2 v = bufB[N - j];
                 rr = v.x;
-                ss = v.y;
+                ss = v.y - goe;
             }
             const int v1 = hh + rr;
             const bool cond = (hh != dd) && (rr == ss);
@@ -400,7 +665,7 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
 
         // Push right then left so the left frame is processed first (:598-609).
         if (sp + 2 > 32) {
-            if (lane == 0) atomicExch(err, 1);
+            if (lane == 0) atomicExch(X.err, 1);
             break;
         }
         if (!type2) {
@@ -421,13 +686,13 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
                 stA = A + midi + 1;
                 stB = B + midj;
                 stM = M - midi - 1;
-                stN = (N - midj) | (0 << 29) | (tef << 30);
+                stN = (N - midj) | (tef << 30);
             }
             if (lane == sp + 1) {
                 stA = A;
                 stB = B;
                 stM = midi - 1;
-                stN = midj | (tbf << 29) | (0 << 30);
+                stN = midj | (tbf << 29);
             }
         }
         sp += 2;
@@ -438,101 +703,122 @@ __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int
     cells = ncell;
 }
 
+struct PairArgs {
+    const int8_t* codes;
+    const int64_t* offs;
+    const int32_t* lens;
+    const int32_t* nres;
+    const int32_t* pairs;
+    const int32_t* order;
+    const int32_t* go_table;
+    const int32_t* matrix;
+    float* dist;
+    cwgpu_pair_stats* stats;
+    int2* scratch;
+    unsigned long long* counter;
+    int* err;
+    unsigned long long* cells;  // [3]: forward, reverse (up to its break), diff
+    long long npairs;
+    int lmax;
+    int ge;
+    int gp1, gp2;  // remapped gap codes
+    int K;         // remapped alphabet size
+    int tiny_m, tiny_n;
+};
+
+// forwardPass + reversePass + diff + distance for one pair, given its 0-based
+// code pointers, lengths, non-gap residue counts and gap penalties. Returns
+// the distance and fills `st`; adds the algorithmic cell counts (the
+// inner-loop iterations the reference executes) to acc[0..2].
+static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int m, int len1, int len2, int go, int ge,
+                           int2* bufA, int2* bufB, const Env& X, cwgpu_pair_stats& st, unsigned long long (&acc)[3]) {
+    st = cwgpu_pair_stats{0, 0, 0, 0, 0, 0, 0, 0};
+    if (n <= 0 || m <= 0) return 1.0f;
+    // forwardPass
+    Task t;
+    t.rseq = s1;
+    t.rdir = 1;
+    t.cseq = s2;
+    t.cdir = 1;
+    t.rows = n;
+    t.cols = m;
+    t.ht0 = 0;
+    t.hts = 0;
+    t.eo = go;
+    t.hl0 = 0;
+    t.hls = 0;
+    t.fo = go;
+    t.buf = bufA;
+    Best fb;
+    sweep<kR, 32, MODE_LOCAL_FWD>(t, go, ge, 0, X, fb);
+    const int max_score = fb.val;
+    const int se1 = max_score > 0 ? (int)(fb.key >> 16) + 1 : 0;
+    const int se2 = max_score > 0 ? (int)(fb.key & 0xffffu) : 0;
+
+    // reversePass
+    int sb1 = 1, sb2 = 1;
+    if (se1 > 0) {
+        Task r;
+        r.rseq = s1 + se1 - 1;
+        r.rdir = -1;
+        r.cseq = s2 + se2 - 1;
+        r.cdir = -1;
+        r.rows = se1;
+        r.cols = se2;
+        r.ht0 = -1;
+        r.hts = 0;
+        r.eo = 0;
+        r.hl0 = -1;
+        r.hls = 0;
+        r.fo = 0;
+        r.buf = bufA;
+        Best rb;
+        sweep<kR, 32, MODE_LOCAL_REV>(r, go, ge, max_score, X, rb);
+        if (rb.val > 0) {
+            sb1 = se1 - (int)(rb.key >> 16);
+            sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
+        }
+        // reversePass stops at the first cell reaching maxScore (:404-413).
+        if (rb.val >= max_score)
+            acc[1] += (unsigned long long)(se1 - sb1) * se2 + (unsigned long long)(se2 - sb2 + 1);
+        else
+            acc[1] += (unsigned long long)se1 * se2;
+    }
+    acc[0] += (unsigned long long)n * m;
+
+    // diff + tracePath
+    int mm = 0, ident = 0, matches = 0;
+    long long dcells = 0;
+    mm_align(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, bufA, bufB, X, mm, ident, matches,
+             dcells);
+    acc[2] += (unsigned long long)dcells;
+
+    // distance (:170-181), float arithmetic with IEEE rounding.
+    float mmv = (float)(100 * ident);
+    if (len1 == 0 || len2 == 0)
+        mmv = 0.0f;
+    else
+        mmv = __fdiv_rn(mmv, (float)min(len1, len2));
+    st.fwd_score = max_score;
+    st.se1 = se1;
+    st.se2 = se2;
+    st.sb1 = sb1;
+    st.sb2 = sb2;
+    st.mm_score = mm;
+    st.n_ident = ident;
+    st.n_match = matches;
+    return __fdiv_rn(__fsub_rn(100.0f, mmv), 100.0f);
+}
+
 // Aligns pair q: FullPairwiseAlign.cpp:112-183 for one (si, sj).
-// Adds the pair's algorithmic cell counts (the inner-loop iterations the
-// reference executes) to acc[0..2].
-template <int R>
-__device__ void align_pair(const PairArgs& g, long long q, uint16_t* prof, const int* smat, int2* bufA,
-                           int2* bufB, unsigned long long (&acc)[3]) {
+static __device__ void align_pair(const PairArgs& g, long long q, const Env& X, int2* bufA, int2* bufB,
+                           unsigned long long (&acc)[3]) {
     const int lane = threadIdx.x & 31;
     const int si = g.pairs[2 * q], sj = g.pairs[2 * q + 1];
     const int n = g.lens[si], m = g.lens[sj];
-    const int8_t* s1 = g.codes + g.offs[si];
-    const int8_t* s2 = g.codes + g.offs[sj];
-    const int go = g.go_table[min(n, m)];
-    const int ge = g.ge;
-    cwgpu_pair_stats st = {0, 0, 0, 0, 0, 0, 0, 0};
-    float dist = 1.0f;
-    if (n > 0 && m > 0) {
-        // forwardPass
-        Task t;
-        t.rseq = s1;
-        t.rdir = 1;
-        t.cseq = s2;
-        t.cdir = 1;
-        t.rows = n;
-        t.cols = m;
-        t.ht0 = 0;
-        t.hts = 0;
-        t.eo = go;
-        t.hl0 = 0;
-        t.hls = 0;
-        t.fo = go;
-        t.buf = bufA;
-        Best fb;
-        sweep<R, 32, MODE_LOCAL_FWD>(t, go, ge, 0, prof, smat, fb);
-        const int max_score = fb.val;
-        const int se1 = max_score > 0 ? (int)(fb.key >> 16) + 1 : 0;
-        const int se2 = max_score > 0 ? (int)(fb.key & 0xffffu) : 0;
-        __syncwarp();
-
-        // reversePass
-        int sb1 = 1, sb2 = 1;
-        if (se1 > 0) {
-            Task r;
-            r.rseq = s1 + se1 - 1;
-            r.rdir = -1;
-            r.cseq = s2 + se2 - 1;
-            r.cdir = -1;
-            r.rows = se1;
-            r.cols = se2;
-            r.ht0 = -1;
-            r.hts = 0;
-            r.eo = 0;
-            r.hl0 = -1;
-            r.hls = 0;
-            r.fo = 0;
-            r.buf = bufA;
-            Best rb;
-            sweep<R, 32, MODE_LOCAL_REV>(r, go, ge, max_score, prof, smat, rb);
-            if (rb.val > 0) {
-                sb1 = se1 - (int)(rb.key >> 16);
-                sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
-            }
-            // reversePass stops at the first cell reaching maxScore (:404-413).
-            if (rb.val >= max_score)
-                acc[1] += (unsigned long long)(se1 - sb1) * se2 + (unsigned long long)(se2 - sb2 + 1);
-            else
-                acc[1] += (unsigned long long)se1 * se2;
-            __syncwarp();
-        }
-        acc[0] += (unsigned long long)n * m;
-
-        // diff + tracePath
-        int mm = 0, ident = 0, matches = 0;
-        long long dcells = 0;
-        mm_align<R>(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, g.gp1, g.gp2, bufA,
-                    bufB, prof, smat, g.err, mm, ident, matches, dcells);
-        acc[2] += (unsigned long long)dcells;
-
-        // distance (:170-181), float arithmetic with IEEE rounding.
-        float mmv = (float)(100 * ident);
-        const int len1 = g.nres[si], len2 = g.nres[sj];
-        if (len1 == 0 || len2 == 0)
-            mmv = 0.0f;
-        else
-            mmv = __fdiv_rn(mmv, (float)min(len1, len2));
-        dist = __fdiv_rn(__fsub_rn(100.0f, mmv), 100.0f);
-
-        st.fwd_score = max_score;
-        st.se1 = se1;
-        st.se2 = se2;
-        st.sb1 = sb1;
-        st.sb2 = sb2;
-        st.mm_score = mm;
-        st.n_ident = ident;
-        st.n_match = matches;
-    }
+    cwgpu_pair_stats st;
+    const float dist = align_one(g.codes + g.offs[si], n, g.codes + g.offs[sj], m, g.nres[si], g.nres[sj],
+                                 g.go_table[min(n, m)], g.ge, bufA, bufB, X, st, acc);
     if (lane == 0) {
         g.dist[q] = dist;
         if (g.stats) g.stats[q] = st;

@@ -32,7 +32,7 @@
 namespace {
 
 constexpr int kNaWarpsPerBlock = 4;
-constexpr size_t kNaProfBytesPerWarp = 32 * 32 * 4 * sizeof(uint16_t);
+constexpr size_t kNaRegionBytes = (size_t)cwgpu::warp_region_bytes(CWGPU_NUMRES);  // per warp, dynamic smem
 constexpr size_t kNaScratchBytes = (size_t)CWGPU_NOALLOC_SCRATCH_BYTES;
 constexpr size_t kNaCtrlBytes = 256;  // [0] queue head, [1..3] cell counts, [4] status word
 constexpr size_t kNaTableBytes = ((size_t)(CWGPU_NOALLOC_MAX_LEN + 1) * sizeof(int32_t) + 255) & ~(size_t)255;
@@ -60,9 +60,8 @@ struct NaArgs {
 // pair index, a length above max_len or a residue code outside [0, 31] sets
 // the status word and the pair is skipped. The residue counts len1/len2 of
 // :100-127 are counted here instead of being uploaded.
-template <int R>
-__device__ void na_align_pair(const NaArgs& a, long long q, uint16_t* prof, const int* smat, int2* bufA,
-                              int2* bufB, unsigned long long (&acc)[3]) {
+__device__ void na_align_pair(const NaArgs& a, long long q, const cwgpu::Env& X, int2* bufA, int2* bufB,
+                              unsigned long long (&acc)[3]) {
     const int lane = threadIdx.x & 31;
     unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(a.scratch);
     int* status = reinterpret_cast<int*>(ctrl + 4);
@@ -95,80 +94,8 @@ __device__ void na_align_pair(const NaArgs& a, long long q, uint16_t* prof, cons
         return;
     }
     const int len1 = __reduce_add_sync(cwgpu::kFull, r1), len2 = __reduce_add_sync(cwgpu::kFull, r2);
-    const int go = go_table[min(n, m)];
-    const int ge = a.ge;
-    cwgpu_pair_stats st = {0, 0, 0, 0, 0, 0, 0, 0};
-    float dist = 1.0f;
-    if (n > 0 && m > 0) {
-        cwgpu::Task t;
-        t.rseq = s1;
-        t.rdir = 1;
-        t.cseq = s2;
-        t.cdir = 1;
-        t.rows = n;
-        t.cols = m;
-        t.ht0 = 0;
-        t.hts = 0;
-        t.eo = go;
-        t.hl0 = 0;
-        t.hls = 0;
-        t.fo = go;
-        t.buf = bufA;
-        cwgpu::Best fb;
-        cwgpu::sweep<R, 32, cwgpu::MODE_LOCAL_FWD>(t, go, ge, 0, prof, smat, fb);
-        const int max_score = fb.val;
-        const int se1 = max_score > 0 ? (int)(fb.key >> 16) + 1 : 0;
-        const int se2 = max_score > 0 ? (int)(fb.key & 0xffffu) : 0;
-        __syncwarp();
-        int sb1 = 1, sb2 = 1;
-        if (se1 > 0) {
-            cwgpu::Task r;
-            r.rseq = s1 + se1 - 1;
-            r.rdir = -1;
-            r.cseq = s2 + se2 - 1;
-            r.cdir = -1;
-            r.rows = se1;
-            r.cols = se2;
-            r.ht0 = -1;
-            r.hts = 0;
-            r.eo = 0;
-            r.hl0 = -1;
-            r.hls = 0;
-            r.fo = 0;
-            r.buf = bufA;
-            cwgpu::Best rb;
-            cwgpu::sweep<R, 32, cwgpu::MODE_LOCAL_REV>(r, go, ge, max_score, prof, smat, rb);
-            if (rb.val > 0) {
-                sb1 = se1 - (int)(rb.key >> 16);
-                sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
-            }
-            if (rb.val >= max_score)
-                acc[1] += (unsigned long long)(se1 - sb1) * se2 + (unsigned long long)(se2 - sb2 + 1);
-            else
-                acc[1] += (unsigned long long)se1 * se2;
-            __syncwarp();
-        }
-        acc[0] += (unsigned long long)n * m;
-        int mm = 0, ident = 0, matches = 0;
-        long long dcells = 0;
-        cwgpu::mm_align<R>(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, a.gp1, a.gp2, bufA,
-                           bufB, prof, smat, status, mm, ident, matches, dcells);
-        acc[2] += (unsigned long long)dcells;
-        float mmv = (float)(100 * ident);
-        if (len1 == 0 || len2 == 0)
-            mmv = 0.0f;
-        else
-            mmv = __fdiv_rn(mmv, (float)min(len1, len2));
-        dist = __fdiv_rn(__fsub_rn(100.0f, mmv), 100.0f);
-        st.fwd_score = max_score;
-        st.se1 = se1;
-        st.se2 = se2;
-        st.sb1 = sb1;
-        st.sb2 = sb2;
-        st.mm_score = mm;
-        st.n_ident = ident;
-        st.n_match = matches;
-    }
+    cwgpu_pair_stats st;
+    const float dist = cwgpu::align_one(s1, n, s2, m, len1, len2, go_table[min(n, m)], a.ge, bufA, bufB, X, st, acc);
     if (lane == 0) {
         a.dist[q] = dist;
         if (a.stats) a.stats[q] = st;
@@ -177,23 +104,31 @@ __device__ void na_align_pair(const NaArgs& a, long long q, uint16_t* prof, cons
 
 __global__ void __launch_bounds__(kNaWarpsPerBlock * 32) k_pairwise_noalloc(NaArgs a) {
     __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
-    __shared__ __align__(16) uint16_t prof_all[kNaWarpsPerBlock * kNaProfBytesPerWarp / sizeof(uint16_t)];
+    extern __shared__ __align__(16) uint16_t na_region[];
     for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = a.matrix[i];
     __syncthreads();
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long slot = (long long)blockIdx.x * kNaWarpsPerBlock + warp;
-    uint16_t* prof = prof_all + (size_t)warp * (kNaProfBytesPerWarp / sizeof(uint16_t));
+    cwgpu::Env X;
+    X.smat = smat;
+    X.region = na_region + (size_t)warp * (kNaRegionBytes / sizeof(uint16_t));
+    X.K = CWGPU_NUMRES;
+    X.gp1 = (a.gp1 >= 0 && a.gp1 < CWGPU_NUMRES) ? a.gp1 : -1;
+    X.gp2 = (a.gp2 >= 0 && a.gp2 < CWGPU_NUMRES) ? a.gp2 : -1;
+    X.tiny_m = 32;
+    X.tiny_n = cwgpu::kTinyMaxN;
+    unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(a.scratch);
+    X.err = reinterpret_cast<int*>(ctrl + 4);
     int2* rows = reinterpret_cast<int2*>(a.scratch + kNaRowsOffset);
     int2* bufA = rows + (size_t)slot * 2 * (a.max_len + 1);
     int2* bufB = bufA + (a.max_len + 1);
-    unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(a.scratch);
     unsigned long long acc[3] = {0, 0, 0};
     for (;;) {
         unsigned long long k = 0;
         if (lane == 0) k = atomicAdd(ctrl, 1ULL);
         k = __shfl_sync(cwgpu::kFull, k, 0);
         if (k >= (unsigned long long)a.npairs) break;
-        na_align_pair<4>(a, (long long)k, prof, smat, bufA, bufB, acc);
+        na_align_pair(a, (long long)k, X, bufA, bufB, acc);
     }
     if (lane == 0 && (acc[0] | acc[1] | acc[2])) {
         atomicAdd(ctrl + 1, acc[0]);
@@ -233,7 +168,11 @@ int na_setup(int dev, NaDevice** out) {
         int sms = 0, per_sm = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise_noalloc, kNaWarpsPerBlock * 32, 0);
+            e = cudaFuncSetAttribute(k_pairwise_noalloc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)(kNaRegionBytes * kNaWarpsPerBlock));
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise_noalloc, kNaWarpsPerBlock * 32,
+                                                              kNaRegionBytes * kNaWarpsPerBlock);
         if (e != cudaSuccess) {
             fprintf(stderr, "cwgpu_align_pairs_noalloc: set-up failed: %s\n", cudaGetErrorString(e));
             return CWGPU_ERR_CUDA;
@@ -306,7 +245,7 @@ extern "C" int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d
         a.ge = ge;
         a.gp1 = params->gap_pos1;
         a.gp2 = params->gap_pos2;
-        k_pairwise_noalloc<<<(unsigned)grid, kNaWarpsPerBlock * 32, 0, s>>>(a);
+        k_pairwise_noalloc<<<(unsigned)grid, kNaWarpsPerBlock * 32, kNaRegionBytes * kNaWarpsPerBlock, s>>>(a);
         e = cudaGetLastError();
     }
     int status = 0;

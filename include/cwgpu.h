@@ -187,6 +187,17 @@ int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d_offsets, c
                               const cwgpu_params* params, const int32_t* d_pairs, int64_t npairs,
                               float* d_dist, cwgpu_pair_stats* d_stats, void* stream);
 
+/* Tuning knobs of the kernel (no reference counterpart; results do not depend
+ * on them). Myers-Miller frames with M <= tiny_m rows and N <= tiny_n columns
+ * (tiny_n <= 16, tiny_m <= 256) are solved one frame per lane instead of by a
+ * warp-wide sweep. The autotuner in clustalw_gb300/autotune.py picks them. */
+typedef struct cwgpu_tuning {
+    int32_t tiny_m;
+    int32_t tiny_n;
+} cwgpu_tuning;
+int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning);
+int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning);
+
 /* Waits for all work of the context and reports a kernel-side error flag. */
 int cwgpu_synchronize(cwgpu_context* ctx);
 
