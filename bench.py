@@ -62,6 +62,10 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=3)
     ap.add_argument("--nseqs", type=int, default=0, help="smaller case of the same family model (profiling)")
     ap.add_argument("--device-only", action="store_true", help="time only the device-resident form (profiling)")
+    ap.add_argument("--serve-seconds", type=float, default=12.0, help="length of the served arrival process")
+    ap.add_argument("--serve-rate", type=float, default=6.0, help="served job arrival rate (jobs/s)")
+    ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--autotune", action="store_true", help="pick the tiny-frame thresholds for this workload first")
     return ap.parse_args()
 
 
@@ -246,6 +250,61 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- served leg
+
+
+def served_leg(args, matrix, params, device):
+    """BASELINE-style served stream: Poisson arrivals of independent protein
+    families (sequence count U[10, 500], root length U[50, 1500]) admitted
+    under a 40 GB budget and mixed in shared rounds; p50/p99 job latency and
+    throughput, next to the plain form that runs the same jobs one at a time."""
+    from clustalw_gb300 import native, synth
+    from clustalw_gb300.serve import Server, percentile, run_arrivals
+
+    njobs = max(4, int(round(args.serve_rate * args.serve_seconds)))
+    spec = synth.serve_jobs(njobs, seed=args.seed)
+    jobs, cells = [], []
+    for n, L, sd in spec:
+        seqs = synth.protein_family(n, L, sd)
+        jobs.append(native.pack_sequences(seqs))
+        lens = np.array([len(x) for x in seqs], dtype=np.int64)
+        cells.append(int((np.sum(lens) ** 2 - np.sum(lens * lens)) // 2))
+    # Plain per-job form: each job alone through the C ABI, one after another.
+    ctx = native.Context(device)
+    ctx.set_matrix(matrix)
+    ctx.set_params(params)
+    sample = list(range(0, njobs, max(1, njobs // 8)))[:8]
+    t_plain, c_plain = 0.0, 0
+    for k in sample:
+        ctx.upload_seqs(packed=jobs[k])
+        pr = synth.all_pairs(len(jobs[k][2]))
+        t = time.perf_counter()
+        ctx.upload_seqs(packed=jobs[k])
+        ctx.align_pairs(pr)
+        t_plain += time.perf_counter() - t
+        c_plain += cells[k]
+    ctx.close()
+    with Server(matrix, params, device=device, memory_budget=40 << 30, max_seq_len=2048, round_cells=6e9) as srv:
+        for k in range(2):  # warm-up jobs
+            srv.wait(srv.submit(packed=jobs[k]))
+        lat, arrivals, wall = run_arrivals(srv, jobs, args.serve_rate, seed=args.seed)
+        info = srv.query()
+    return {
+        "rate_jobs_per_s": args.serve_rate,
+        "jobs": njobs,
+        "arrival_seconds": float(arrivals[-1]),
+        "p50_ms": 1e3 * percentile(lat, 50),
+        "p99_ms": 1e3 * percentile(lat, 99),
+        "mean_ms": 1e3 * float(np.mean(lat)),
+        "gcups": sum(cells) / wall / 1e9,
+        "plain_per_job_gcups": c_plain / t_plain / 1e9,
+        "plain_sample_jobs": len(sample),
+        "rounds": info["rounds"],
+        "budget_bytes": 40 << 30,
+        "workload": "protein families, N ~ U[10,500], root length ~ U[50,1500], Poisson arrivals",
+    }
+
+
 # ---------------------------------------------------------------- GPU arm
 
 
@@ -288,6 +347,13 @@ def ours_arm(args):
     ctx.set_matrix(matrix)
     ctx.set_params(params)
     ctx.upload_seqs(packed=packed)
+    tuning = {"tiny_m_tiny_n": list(ctx.get_tuning()), "autotuned": False}
+    if args.autotune:
+        from clustalw_gb300 import autotune
+
+        choice, timings = autotune.tune(ctx, packed[2], pairs, gpu_name=torch.cuda.get_device_name(local))
+        tuning = {"tiny_m_tiny_n": list(choice), "autotuned": True,
+                  "candidates_s": {f"{m},{n}": round(t, 4) for (m, n), t in timings.items()}}
     plan = ctx.plan(pairs)
     # A dedicated stream: the graph is launched on it and the CUDA events are
     # recorded on it (torch's default stream has handle 0, which the C ABI
@@ -412,6 +478,7 @@ def ours_arm(args):
             "form": "batched: persistent graph-captured launch, longest pairs first",
             "l2": "flushed between timed steps (256 MiB write, untimed)",
             "pairs_per_s": len(pairs) * world / (ms / 1e3),
+            "tuning": tuning,
         },
         "e2e": {
             "value": cells_nm / e2e_s / 1e9,
@@ -436,6 +503,8 @@ def ours_arm(args):
             line["clocks"] = clocks
         if world == 1:
             line["cpu_baseline"] = cpu_baseline(seqs, matrix, params, pairs, args.cpu_seconds)
+            if not args.no_serve:
+                line["serve"] = served_leg(args, matrix, params, local)
         print(json.dumps(line), flush=True)
     plan.close()
     ctx.close()

@@ -14,7 +14,7 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcwgpu.so")
 
-SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu"]
+SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu", "cwgpu_serve.cu"]
 HEADERS = ["cwgpu_device.cuh"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -56,6 +56,8 @@ def build(force=False, verbose=False):
     ]
     if verbose:
         cmd.insert(1, "-Xptxas=-v")
+    # Translation units compile in parallel (-t), one -gencode.
+    cmd.insert(1, "-t0")
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB_PATH)
     return LIB_PATH

@@ -77,6 +77,28 @@ class Tuning(ctypes.Structure):
     _fields_ = [("tiny_m", ctypes.c_int32), ("tiny_n", ctypes.c_int32)]
 
 
+class ServerOpts(ctypes.Structure):
+    _fields_ = [
+        ("memory_budget_bytes", ctypes.c_int64),
+        ("max_jobs", ctypes.c_int32),
+        ("max_seq_len", ctypes.c_int32),
+        ("round_cells", ctypes.c_double),
+        ("max_items_per_round", ctypes.c_int64),
+    ]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [
+        ("jobs_queued", ctypes.c_int64),
+        ("jobs_running", ctypes.c_int64),
+        ("jobs_done", ctypes.c_int64),
+        ("rounds", ctypes.c_int64),
+        ("pairs", ctypes.c_int64),
+        ("bytes_in_use", ctypes.c_int64),
+        ("cells", ctypes.c_int64 * 3),
+    ]
+
+
 _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
@@ -107,6 +129,17 @@ SIGNATURES = {
     "cwgpu_synchronize": (ctypes.c_int, [_vp]),
     "cwgpu_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
     "cwgpu_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
+    "cwgpu_server_create": (
+        ctypes.c_int,
+        [ctypes.c_int, _vp, ctypes.POINTER(Params), ctypes.POINTER(ServerOpts), ctypes.POINTER(_vp)],
+    ),
+    "cwgpu_server_destroy": (None, [_vp]),
+    "cwgpu_server_submit": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _i32, ctypes.POINTER(_i64)]),
+    "cwgpu_server_poll": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(_i32)]),
+    "cwgpu_server_wait": (ctypes.c_int, [_vp, _i64, _i32]),
+    "cwgpu_server_result": (ctypes.c_int, [_vp, _i64, _vp, _vp, _vp]),
+    "cwgpu_server_release": (ctypes.c_int, [_vp, _i64]),
+    "cwgpu_server_query": (ctypes.c_int, [_vp, ctypes.POINTER(ServerStats)]),
     "cwgpu_align_pairs_noalloc": (
         ctypes.c_int,
         [_vp, _vp, _vp, _i32, _i32, _vp, ctypes.POINTER(Params), _vp, _i64, _vp, _vp, _vp],

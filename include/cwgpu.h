@@ -198,6 +198,51 @@ typedef struct cwgpu_tuning {
 int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning);
 int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning);
 
+/* ---- serving: continuous batching of independent jobs -----------------------
+ * No counterpart in the reference (which aligns one sequence set per call).
+ * A server owns one device, one scoring scheme (the matrix and params of
+ * cwgpu_set_matrix/cwgpu_set_params) and a device-memory budget. Submitted
+ * jobs (sequence sets; each job's result is what cwgpu_align_pairs returns
+ * for all of its pairs in the reference's loop order) are admitted in arrival
+ * order as job slots and budget memory free up; their sequences and distances
+ * stay resident until released. A scheduler thread runs rounds: one persistent
+ * launch over pairs mixed from every admitted job, two rounds in flight, so
+ * jobs that arrive while others run join the next round. */
+enum { CWGPU_JOB_QUEUED = 0, CWGPU_JOB_RUNNING = 1, CWGPU_JOB_DONE = 2, CWGPU_JOB_FAILED = 3 };
+typedef struct cwgpu_server_opts {
+    int64_t memory_budget_bytes; /* arena for resident job data and results */
+    int32_t max_jobs;            /* job slots */
+    int32_t max_seq_len;         /* longest sequence a job may hold */
+    double round_cells;          /* sum of n*m per round (work granularity) */
+    int64_t max_items_per_round; /* pairs per round */
+} cwgpu_server_opts;
+typedef struct cwgpu_server_stats {
+    int64_t jobs_queued, jobs_running, jobs_done;
+    int64_t rounds, pairs;
+    int64_t bytes_in_use;
+    int64_t cells[3]; /* forward, reverse, diff cell updates so far */
+} cwgpu_server_stats;
+typedef struct cwgpu_server cwgpu_server;
+int cwgpu_server_create(int device, const int32_t* matrix, const cwgpu_params* params,
+                        const cwgpu_server_opts* opts, cwgpu_server** out);
+/* Stops admitting, finishes admitted jobs, frees everything. */
+void cwgpu_server_destroy(cwgpu_server* server);
+/* Copies the job's sequences (same layout as cwgpu_upload_seqs) and queues
+ * it. CWGPU_ERR_OOM if the job can never fit the budget. */
+int cwgpu_server_submit(cwgpu_server* server, int32_t nseqs, const int8_t* codes, const int64_t* offsets,
+                        const int32_t* lens, int32_t want_stats, int64_t* job_id);
+int cwgpu_server_poll(cwgpu_server* server, int64_t job_id, int32_t* state);
+/* Blocks until the job is done (timeout_ms < 0: no limit; else
+ * CWGPU_ERR_TIMEOUT when it runs out). */
+int cwgpu_server_wait(cwgpu_server* server, int64_t job_id, int32_t timeout_ms);
+/* Distances (N(N-1)/2, loop order), stats (if submitted with want_stats) and
+ * times[4] = submit, admit, first round, done (seconds, steady clock). */
+int cwgpu_server_result(cwgpu_server* server, int64_t job_id, float* dist_out, cwgpu_pair_stats* stats_out,
+                        double* times);
+/* Frees the job's device memory and slot. */
+int cwgpu_server_release(cwgpu_server* server, int64_t job_id);
+int cwgpu_server_query(cwgpu_server* server, cwgpu_server_stats* out);
+
 /* Waits for all work of the context and reports a kernel-side error flag. */
 int cwgpu_synchronize(cwgpu_context* ctx);
 

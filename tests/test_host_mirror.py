@@ -1,0 +1,90 @@
+"""The Python mirror of the reference's pairwise plugin interface
+(clustalw_gb300.pairwise): SymMatrix index rule and bounds, the reference's
+error behaviour for a wrong matrix size and bad ranges (message + exit 1, no
+device work), residue encoding, and -- on the GPU -- pairwiseAlign filling a
+DistMatrix exactly as the reference's FullPairwiseAlign did (golden fixtures,
+full and partial ranges), with the same per-pair info lines."""
+import numpy as np
+import pytest
+
+from conftest import load_golden, range_pairs, sym_index
+
+
+def test_symmatrix_index_rule():
+    from clustalw_gb300.pairwise import SymMatrix
+
+    m = SymMatrix(7)  # 6 sequences
+    seen = set()
+    for i in range(1, 7):
+        for j in range(1, 7):
+            k = m.getIndex(i, j)
+            assert k == m.getIndex(j, i)
+            if i != j:
+                seen.add(k)
+    assert m.getIndex(0, 3) == 0 and m.getIndex(3, 0) == 0
+    assert len(seen) == 15
+    pairs = np.array([(a, b) for a in range(6) for b in range(a + 1, 6)])
+    assert sorted(seen) == sorted(sym_index(pairs).tolist())
+    with pytest.raises(IndexError):
+        m.getIndex(7, 1)
+    m.SetAt(2, 5, 0.25)
+    assert m.GetAt(5, 2) == 0.25
+
+
+def test_reference_error_behaviour(capsys):
+    from clustalw_gb300.pairwise import Alignment, DistMatrix, FullPairwiseAlign, PairwiseSettings
+
+    g = load_golden("synth_uneven_40")
+    aln = Alignment(g["seqs"][:5])
+    fpa = FullPairwiseAlign(PairwiseSettings(g["matrix"], g["params"]))
+    with pytest.raises(SystemExit) as e:
+        fpa.pairwiseAlign(aln, DistMatrix(5), 0, 5, 0, 5)  # needs size 6
+    assert e.value.code == 1
+    assert "The distance matrix is not the right size!" in capsys.readouterr().out
+    for rng in [(-1, 5, 0, 5), (3, 2, 0, 5), (0, 5, -1, 5), (0, 5, 4, 3)]:
+        with pytest.raises(SystemExit) as e:
+            fpa.pairwiseAlign(aln, DistMatrix(6), *rng)
+        assert e.value.code == 1
+        assert "The range for pairwise Alignment is incorrect." in capsys.readouterr().out
+    # No sequences: returns without touching the device.
+    fpa.pairwiseAlign(Alignment([]), DistMatrix(1), 0, 0, 0, 0)
+
+
+def test_encode_decode():
+    from clustalw_gb300.pairwise import GAP_POS2, decode, encode
+
+    c = encode("ACDEFGHIKLMNPQRSTVWYbzx-")
+    assert c[-1] == GAP_POS2 and c[0] == 0 and c[1] == 2
+    assert decode(c) == "ACDEFGHIKLMNPQRSTVWYBZX-"
+    with pytest.raises(ValueError):
+        encode("AJ")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["fixture_100_97", "range_100_97_cols49", "range_100_97_block", "edge_protein"])
+def test_pairwise_align_fills_distmatrix_like_reference(name):
+    from clustalw_gb300.pairwise import Alignment, DistMatrix, FullPairwiseAlign, PairwiseSettings
+
+    g = load_golden(name)
+    aln = Alignment(g["seqs"])
+    dm = DistMatrix(aln.getNumSeqs() + 1)
+    FullPairwiseAlign(PairwiseSettings(g["matrix"], g["params"])).pairwiseAlign(aln, dm, *g["range"])
+    assert np.array_equal(dm.getElements(), g["elements"])
+
+
+@pytest.mark.gpu
+def test_info_lines(capsys):
+    from clustalw_gb300.pairwise import Alignment, DistMatrix, FullPairwiseAlign, PairwiseSettings
+
+    g = load_golden("fixture_100_97")
+    seqs = g["seqs"][:6]
+    aln = Alignment(seqs)
+    dm = DistMatrix(7)
+    FullPairwiseAlign(PairwiseSettings(g["matrix"], g["params"], display_info=True)).pairwiseAlign(aln, dm, 0, 6, 0, 6)
+    lines = [l for l in capsys.readouterr().out.splitlines() if l.startswith("Sequences (")]
+    assert len(lines) == 15
+    for line in lines:  # percent identity = (1 - d) * 100 truncated, from the same float arithmetic
+        i, j = (int(x) for x in line.split("(")[1].split(")")[0].split(":"))
+        score = int(line.rsplit(" ", 1)[1])
+        d = dm.GetAt(i, j)
+        assert abs((100.0 - 100.0 * d) - score) < 1.0 + 1e-4

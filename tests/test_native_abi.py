@@ -62,3 +62,17 @@ def test_range_pair_count(lib):
 def test_status_strings(lib):
     for code in range(10):
         assert lib.cwgpu_status_string(code)
+
+
+def test_autotune_helpers_cpu():
+    from clustalw_gb300 import autotune, synth
+
+    rng = np.random.default_rng(3)
+    lens = rng.integers(30, 2000, size=200)
+    pairs = synth.all_pairs(200)
+    s = autotune.stratified_sample(lens, pairs, 5e8)
+    assert len(s) > 0 and s.shape[1] == 2
+    work = lens[s[:, 0]].astype(np.int64) * lens[s[:, 1]]
+    assert work.min() < np.median(lens) ** 2 < work.max()
+    assert autotune.length_profile(lens) == autotune.length_profile(lens.copy())
+    assert autotune.length_profile([1523] * 10) != autotune.length_profile([97] * 10)
