@@ -26,7 +26,7 @@ general/VectorOutOfRange general/InvalidCombination general/DebugLog general/Sta
 general/ClustalWResources general/OutputFile fileInput/FileReader fileInput/FileParser
 fileInput/PearsonFileParser fileInput/InFileStream fileInput/MSFFileParser
 fileInput/PIRFileParser fileInput/RSFFileParser fileInput/GDEFileParser
-fileInput/ClustalFileParser fileInput/EMBLFileParser"
+fileInput/ClustalFileParser fileInput/EMBLFileParser tree/NJTree"
 OBJS=""
 for u in $UNITS; do
     o="$OUT/obj/$(basename "$u").o"

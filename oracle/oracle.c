@@ -454,3 +454,185 @@ int cwo_align_pairs(const int8_t* codes, const int64_t* offsets, const int32_t* 
     pthread_mutex_destroy(&j.mu);
     return rc;
 }
+
+/* ------------------------------------------------------------ guide tree */
+
+/* SymMatrix::getIndex (general/SymMatrix.h:166-197) for 1-based i, j. */
+static size_t sym_idx(int i, int j) {
+    if (i == 0 || j == 0) return 0;
+    int a = i - 1, b = j - 1;
+    if (a == b) return ((size_t)a * (a + 3)) >> 1;
+    if (a < b) {
+        int t = a;
+        a = b;
+        b = t;
+    }
+    return (((size_t)a * (a + 1)) >> 1) + b;
+}
+
+/* Neighbour joining, NJTree::generateTree (tree/NJTree.cpp:161-748) with
+ * firstSeq = 1, lastSeq = n, as UnRootedClusterTree::treeFromDistMatrix calls
+ * it. d: packed SymMatrix elements of size n+1, updated in place like the
+ * reference. left/right: n+2 doubles; desc: (n+1)*(n+1) ints, row-major.
+ * Valid nodes are kept in ascending order, which is the order the reference's
+ * linked list visits them. Returns 0, or 1 if n < 2. */
+int cwo_nj_tree(int n, double* d, double* left, double* right, int32_t* desc) {
+    if (n < 2) return 1;
+    if (n == 2) return 0; /* :218-229 returns before touching the tree */
+    const int W = n + 1;
+    double* sumCols = (double*)calloc(n + 1, sizeof(double));
+    double* sumRows = (double*)calloc(n + 1, sizeof(double));
+    double* join = (double*)calloc(n + 1, sizeof(double));
+    double* av = (double*)calloc(n + 1, sizeof(double));
+    char* valid = (char*)calloc(n + 2, 1);
+    int i, j, ii, jj, nc, mini, minj;
+    double fnseqs = (double)n, fnseqs2 = 0, sumd, tmin, total, diq, djq, dij, dio, djo, dmin, bi, bj, da;
+    for (i = 0; i < n + 2; i++) left[i] = right[i] = 0.0;
+    memset(desc, 0, sizeof(int32_t) * (size_t)W * W);
+    for (i = 1; i <= n; i++) {
+        d[sym_idx(i, i)] = av[i] = 0.0;
+        valid[i] = 1;
+    }
+    for (j = 1; j <= n; j++) {
+        double s = 0.0;
+        for (i = 1; i < j; i++) s = s + d[sym_idx(i, j)];
+        sumRows[j] = s;
+        s = 0.0;
+        for (i = j + 1; i <= n; i++) s += d[sym_idx(j, i)];
+        sumCols[j] = s;
+    }
+    for (nc = 1; nc <= n - 3; ++nc) {
+        sumd = 0.0;
+        for (j = 1; j <= n; j++)
+            if (valid[j]) sumd += sumCols[j];
+        fnseqs2 = fnseqs - 2.0;
+        tmin = 99999.0 * 2.0 * fnseqs2;
+        mini = minj = 0;
+        for (jj = 2; jj <= n; jj++) {
+            if (!valid[jj]) continue;
+            for (ii = 1; ii < jj; ii++) {
+                if (!valid[ii]) continue;
+                diq = sumCols[ii] + sumRows[ii];
+                djq = sumCols[jj] + sumRows[jj];
+                dij = d[sym_idx(ii, jj)];
+                total = fnseqs2 * dij + 2.0 * sumd - diq - djq;
+                if (total < tmin) {
+                    tmin = total;
+                    mini = ii;
+                    minj = jj;
+                }
+            }
+        }
+        dio = sumCols[mini] + sumRows[mini];
+        djo = sumCols[minj] + sumRows[minj];
+        dmin = d[sym_idx(mini, minj)];
+        dio = (dio - dmin) / fnseqs2;
+        djo = (djo - dmin) / fnseqs2;
+        bi = (dmin + dio - djo) * 0.5;
+        bj = dmin - bi;
+        bi = bi - av[mini];
+        bj = bj - av[minj];
+        const int typei = av[mini] > 0.0 ? 0 : 1, typej = av[minj] > 0.0 ? 0 : 1;
+        if (fabs(bi) < 0.0001) bi = 0.0;
+        if (fabs(bj) < 0.0001) bj = 0.0;
+        left[nc] = bi;
+        right[nc] = bj;
+        for (i = 1; i <= n; i++) desc[(size_t)nc * W + i] = 0;
+        const int who[2] = {mini, minj}, typ[2] = {typei, typej};
+        for (int side = 0; side < 2; side++) {
+            if (typ[side] == 0) {
+                for (i = nc - 1; i >= 1; i--)
+                    if (desc[(size_t)i * W + who[side]] == 1) {
+                        for (j = 1; j <= n; j++)
+                            if (desc[(size_t)i * W + j] == 1) desc[(size_t)nc * W + j] = 1;
+                        break;
+                    }
+            } else {
+                desc[(size_t)nc * W + who[side]] = 1;
+            }
+        }
+        if (dmin <= 0.0) dmin = 0.000001;
+        av[mini] = dmin * 0.5;
+        fnseqs = fnseqs - 1.0;
+        valid[minj] = 0;
+        for (j = 1; j <= n; j++) {
+            if (!valid[j]) continue;
+            double tmp_di = 0.0, tmp_dj = 0.0;
+            if (j < minj) {
+                tmp_dj = d[sym_idx(j, minj)];
+                sumCols[j] -= tmp_dj;
+            } else if (j > minj) {
+                tmp_dj = d[sym_idx(minj, j)];
+                sumRows[j] -= tmp_dj;
+            }
+            if (j < mini) {
+                tmp_di = d[sym_idx(j, mini)];
+                sumCols[j] -= tmp_di;
+            } else if (j > mini) {
+                tmp_di = d[sym_idx(mini, j)];
+                sumRows[j] -= tmp_di;
+            }
+            join[j] = (tmp_dj + tmp_di) * 0.5;
+        }
+        for (j = 1; j <= n; j++) {
+            if (!valid[j]) continue;
+            if (j < mini) {
+                d[sym_idx(j, mini)] = join[j];
+                sumCols[j] += join[j];
+            } else if (j > mini) {
+                d[sym_idx(mini, j)] = join[j];
+                sumRows[j] += join[j];
+            }
+        }
+        sumCols[mini] = sumRows[mini] = 0.0;
+        da = 0.0;
+        for (j = 1; j < mini; j++)
+            if (valid[j]) da = da + join[j];
+        sumRows[mini] = da;
+        da = 0.0;
+        for (j = mini + 1; j <= n; j++)
+            if (valid[j]) da = da + join[j];
+        sumCols[mini] = da;
+        sumCols[minj] = sumRows[minj] = 0.0;
+        for (j = 1; j <= n; ++j) {
+            d[sym_idx(minj, j)] = 0.0;
+            d[sym_idx(j, minj)] = 0.0;
+            join[j] = 0.0;
+        }
+    }
+    /* last cycle: three nodes left (:646-737) */
+    int l[4], nude = 1;
+    for (i = 1; i <= n; i++)
+        if (valid[i]) l[nude++] = i;
+    double b1 = (d[sym_idx(l[1], l[2])] + d[sym_idx(l[1], l[3])] - d[sym_idx(l[2], l[3])]) * 0.5;
+    double b2 = d[sym_idx(l[1], l[2])] - b1;
+    double b3 = d[sym_idx(l[1], l[3])] - b1;
+    double branch[4];
+    branch[1] = b1 - av[l[1]];
+    branch[2] = b2 - av[l[2]];
+    branch[3] = b3 - av[l[3]];
+    for (i = 1; i <= 3; i++)
+        if (fabs(branch[i]) < 0.0001) branch[i] = 0.0;
+    left[n - 2] = branch[1];
+    left[n - 1] = branch[2];
+    left[n] = branch[3];
+    for (i = 1; i <= n; i++) desc[(size_t)(n - 2) * W + i] = 0;
+    for (i = 1; i <= 3; ++i) {
+        if (av[l[i]] > 0.0) {
+            for (int k = n - 3; k >= 1; k--)
+                if (desc[(size_t)k * W + l[i]] == 1) {
+                    for (j = 1; j <= n; j++)
+                        if (desc[(size_t)k * W + j] == 1) desc[(size_t)(n - 2) * W + j] = i;
+                    break;
+                }
+        } else {
+            desc[(size_t)(n - 2) * W + l[i]] = i;
+        }
+    }
+    free(sumCols);
+    free(sumRows);
+    free(join);
+    free(av);
+    free(valid);
+    return 0;
+}

@@ -82,6 +82,8 @@ def lib():
             ctypes.c_void_p,
             ctypes.c_int32,
         ]
+        L.cwo_nj_tree.restype = ctypes.c_int
+        L.cwo_nj_tree.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.cwo_gap_penalties.restype = None
         L.cwo_gap_penalties.argtypes = [
             ctypes.POINTER(Params),
@@ -139,6 +141,43 @@ def align_pairs(seqs, matrix, params, pairs, nthreads=None):
     if rc != 0:
         raise RuntimeError(f"cwo_align_pairs failed with {rc}")
     return out
+
+
+def nj_tree(n, elements):
+    """NJTree::generateTree restated (oracle.c cwo_nj_tree). Returns
+    (left_branch[n+2], right_branch[n+2], tree_desc[(n+1),(n+1)], elements_after)."""
+    d = np.ascontiguousarray(np.array(elements, dtype=np.float64))
+    left = np.zeros(n + 2, dtype=np.float64)
+    right = np.zeros(n + 2, dtype=np.float64)
+    desc = np.zeros((n + 1) * (n + 1), dtype=np.int32)
+    rc = lib().cwo_nj_tree(int(n), d.ctypes.data, left.ctypes.data, right.ctypes.data, desc.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("cwo_nj_tree failed")
+    return left, right, desc.reshape(n + 1, n + 1), d
+
+
+def run_reference_nj(n, elements, workdir):
+    """Run the reference NJTree through the harness (built here only)."""
+    inp = os.path.join(workdir, "nj_in.bin")
+    out = os.path.join(workdir, "nj_out.bin")
+    with open(inp, "wb") as f:
+        f.write(np.int32(n).tobytes())
+        f.write(np.asarray(elements, dtype="<f8").tobytes())
+    subprocess.run([REF_HARNESS, "--nj", inp, out], check=True, stdout=subprocess.DEVNULL)
+    with open(out, "rb") as f:
+        buf = f.read()
+    off = 4
+    left = np.frombuffer(buf, "<f8", n + 2, off).copy()
+    off += 8 * (n + 2)
+    right = np.frombuffer(buf, "<f8", n + 2, off).copy()
+    off += 8 * (n + 2)
+    desc = np.frombuffer(buf, "<i4", (n + 1) * (n + 1), off).copy().reshape(n + 1, n + 1)
+    off += 4 * (n + 1) * (n + 1)
+    nel = (n + 1) * (n + 2) // 2
+    el = np.frombuffer(buf, "<f8", nel, off).copy()
+    off += 8 * nel
+    secs = float(np.frombuffer(buf, "<f8", 1, off)[0])
+    return left, right, desc, el, secs
 
 
 def gap_penalties(params, n, m):

@@ -12,6 +12,14 @@
 // DistMatrix sized numSeqs+1, then one pairwiseAlign(iStart, iEnd, jStart, jEnd).
 //
 // Usage: refharness IN.fa OUT.bin [iStart iEnd jStart jEnd]
+//        refharness --nj IN.dist OUT.tree
+//
+// --nj runs clustalw::NJTree::generateTree (tree/NJTree.cpp:161-748) the way
+// UnRootedClusterTree::treeFromDistMatrix calls it (tree/UnRootedClusterTree.cpp:
+// 236-245): IN.dist is int32 n followed by the packed SymMatrix elements
+// (double[(n+1)(n+2)/2]); OUT.tree is int32 n, double leftBranch[n+2],
+// double rightBranch[n+2], int32 treeDesc[(n+1)*(n+1)], and the SymMatrix
+// elements as generateTree leaves them (it works in place).
 //
 // OUT.bin layout (little endian):
 //   char[8]  "CWREF01\0"
@@ -39,6 +47,7 @@
 #include "general/clustalw.h"
 #include "pairwise/FullPairwiseAlign.h"
 #include "substitutionMatrix/SubMatrix.h"
+#include "tree/NJTree.h"
 
 namespace clustalw {
 UserParameters* userParameters;
@@ -57,7 +66,47 @@ static void put(FILE* f, const void* p, size_t n) {
     }
 }
 
+static int run_nj(const char* in, const char* out) {
+    FILE* f = fopen(in, "rb");
+    if (!f) return 4;
+    int n = 0;
+    if (fread(&n, sizeof(int), 1, f) != 1 || n < 2) return 5;
+    SymMatrix dist;
+    dist.ResizeRect(n + 1);
+    size_t nel = (size_t)(n + 1) * (n + 2) / 2;
+    if (fread(dist.getElements(), sizeof(double), nel, f) != nel) return 5;
+    fclose(f);
+    PhyloTree tree;
+    tree.treeDesc.resize(n + 1, std::vector<int>(n + 1));
+    SeqInfo info;
+    info.firstSeq = 1;
+    info.lastSeq = n;
+    info.numSeqs = n;
+    NJTree nj;
+    auto t0 = std::chrono::steady_clock::now();
+    nj.generateTree(&tree, &dist, &info);
+    double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    tree.leftBranch.resize(n + 2, 0.0);
+    tree.rightBranch.resize(n + 2, 0.0);
+    FILE* g = fopen(out, "wb");
+    if (!g) return 4;
+    put(g, &n, sizeof(int));
+    put(g, tree.leftBranch.data(), sizeof(double) * (n + 2));
+    put(g, tree.rightBranch.data(), sizeof(double) * (n + 2));
+    for (int i = 0; i <= n; ++i) put(g, tree.treeDesc[i].data(), sizeof(int) * (n + 1));
+    put(g, dist.getElements(), sizeof(double) * nel);
+    put(g, &secs, sizeof(secs));
+    fclose(g);
+    printf("refharness: NJ on %d sequences, %.6f s\n", n, secs);
+    return 0;
+}
+
 int main(int argc, char** argv) {
+    if (argc == 4 && std::string(argv[1]) == "--nj") {
+        userParameters = new UserParameters(false);
+        utilityObject = new Utility();
+        return run_nj(argv[2], argv[3]);
+    }
     if (argc != 3 && argc != 7) {
         fprintf(stderr, "usage: %s IN.fa OUT.bin [iStart iEnd jStart jEnd]\n", argv[0]);
         return 2;

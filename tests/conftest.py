@@ -45,7 +45,19 @@ def load_golden(name):
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+    """Distance-stage fixtures (the guide-tree fixtures start with nj_)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("nj_"))
+
+
+def nj_golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("nj_") and f.endswith(".npz"))
+
+
+def load_nj_golden(name):
+    """A guide-tree fixture: the reference NJTree::generateTree run on a packed
+    DistMatrix (tree/NJTree.cpp:161-748)."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    return {k: z[k] for k in z.files}
 
 
 def range_pairs(n, i0, i1, j0, j1):

@@ -58,6 +58,40 @@ def run_fasta(text, name, rng=None):
         return O.run_reference(fa, os.path.join(d, "out.bin"), rng)
 
 
+def save_nj(name, n, elements):
+    with tempfile.TemporaryDirectory() as d:
+        left, right, desc, el, secs = O.run_reference_nj(n, elements, d)
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), n=np.int32(n), elements=np.asarray(elements, np.float64),
+                        left=left, right=right, desc=desc, elements_after=el)
+    print(f"{name}: NJ on {n} sequences, ref {secs:.4f}s")
+
+
+def make_nj():
+    """Guide trees (NJTree::generateTree) of the reference's own distance matrices,
+    plus small and tie-heavy matrices."""
+    import glob
+
+    for path in sorted(glob.glob(os.path.join(OUT, "fixture_*.npz"))) + [os.path.join(OUT, "synth_uneven_40.npz")]:
+        z = np.load(path)
+        n = len(z["lens"])
+        save_nj("nj_" + os.path.basename(path)[:-4], n, z["elements"])
+    rng = np.random.default_rng(7)
+    for n in (3, 4, 5, 9):
+        el = np.zeros((n + 1) * (n + 2) // 2)
+        for i in range(1, n + 1):
+            for j in range(1, i):
+                el[(i - 1) * i // 2 + (j - 1)] = float(np.float32(rng.uniform(0.05, 0.9)))
+        save_nj(f"nj_random_{n}", n, el)
+    # Ties: groups of identical sequences (distance 0) and repeated distances.
+    n = 30
+    grp = rng.integers(0, 6, size=n)
+    el = np.zeros((n + 1) * (n + 2) // 2)
+    for i in range(1, n + 1):
+        for j in range(1, i):
+            el[(i - 1) * i // 2 + (j - 1)] = 0.0 if grp[i - 1] == grp[j - 1] else float(np.float32(0.1 * (1 + (grp[i - 1] + grp[j - 1]) % 4)))
+    save_nj("nj_ties_30", n, el)
+
+
 def main():
     O.build()
     mats = {}
@@ -107,6 +141,8 @@ def main():
     text = "".join(f">e{i}\n{s}\n" for i, s in enumerate(edge))
     save("edge_protein", run_fasta(text, "e"))
 
+    make_nj()
+
     os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
     with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
         json.dump(mats, f, indent=0)
@@ -114,4 +150,8 @@ def main():
 
 
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "--nj-only":
+        O.build()
+        make_nj()
+    else:
+        main()

@@ -1,0 +1,42 @@
+"""The guide-tree restatement (oracle.c cwo_nj_tree) against the unmodified
+reference NJTree::generateTree (tree/NJTree.cpp:161-748), run by
+tests/golden/make_golden.py on the reference's own distance matrices, small
+matrices (N = 3, 4, 5, 9) and a matrix full of ties. Bit-exact: branch lengths,
+the treeDesc membership table and the distance matrix the reference leaves
+behind (it joins in place)."""
+import numpy as np
+import pytest
+
+from conftest import load_nj_golden, nj_golden_names
+
+
+def same_bits(a, b):
+    return np.array_equal(np.asarray(a, np.float64).view(np.int64), np.asarray(b, np.float64).view(np.int64))
+
+
+@pytest.mark.parametrize("name", nj_golden_names())
+def test_nj_oracle_matches_reference(name, oracle_mod):
+    g = load_nj_golden(name)
+    n = int(g["n"])
+    left, right, desc, after = oracle_mod.nj_tree(n, g["elements"])
+    assert same_bits(left, g["left"])
+    assert same_bits(right, g["right"])
+    assert np.array_equal(desc, g["desc"])
+    assert same_bits(after, g["elements_after"])
+
+
+def test_nj_golden_has_ties():
+    """The tie fixture really exercises the first-minimum rule: several pairs
+    share the minimum of the first cycle's criterion."""
+    g = load_nj_golden("nj_ties_30")
+    n = int(g["n"])
+    el = g["elements"]
+
+    def d(i, j):
+        a, b = max(i, j) - 1, min(i, j) - 1
+        return el[a * (a + 1) // 2 + b]
+
+    r = [0.0] + [sum(d(i, j) for j in range(1, n + 1) if j != i) for i in range(1, n + 1)]
+    s = sum(d(i, j) for j in range(1, n + 1) for i in range(1, j))
+    tot = [(n - 2) * d(i, j) + 2 * s - r[i] - r[j] for j in range(2, n + 1) for i in range(1, j)]
+    assert sum(1 for t in tot if t == min(tot)) > 1
