@@ -14,7 +14,7 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcwgpu.so")
 
-SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu", "cwgpu_serve.cu"]
+SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu", "cwgpu_serve.cu", "cwgpu_nj.cu"]
 HEADERS = ["cwgpu_device.cuh"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
@@ -30,7 +30,7 @@ def _stale():
     if not os.path.exists(LIB_PATH):
         return True
     t = os.path.getmtime(LIB_PATH)
-    deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS] + [os.path.join(INCLUDE, "cwgpu.h")]
+    deps = [os.path.join(CSRC, s) for s in SOURCES + HEADERS] + [os.path.join(INCLUDE, h) for h in ("cwgpu.h", "cwgpu_nj.h")]
     return any(os.path.getmtime(d) > t for d in deps)
 
 

@@ -103,7 +103,7 @@ _vp = ctypes.c_void_p
 _i32 = ctypes.c_int32
 _i64 = ctypes.c_int64
 
-# name -> (restype, argtypes); every function include/cwgpu.h declares.
+# name -> (restype, argtypes); every function include/*.h declares.
 SIGNATURES = {
     "cwgpu_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
     "cwgpu_destroy": (None, [_vp]),
@@ -144,6 +144,14 @@ SIGNATURES = {
         ctypes.c_int,
         [_vp, _vp, _vp, _i32, _i32, _vp, ctypes.POINTER(Params), _vp, _i64, _vp, _vp, _vp],
     ),
+    # include/cwgpu_nj.h
+    "cwgpu_nj_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
+    "cwgpu_nj_destroy": (None, [_vp]),
+    "cwgpu_nj_last_error": (ctypes.c_char_p, [_vp]),
+    "cwgpu_nj_tree": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp]),
+    "cwgpu_nj_tree_device": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "cwgpu_nj_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(ctypes.c_double)]),
+    "cwgpu_nj_seq_sum": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
 }
 
 _lib = None
