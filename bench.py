@@ -18,6 +18,9 @@ divided by the time of the step.
   roofline   INT32-issue roofline of the one kernel (k_pairwise)
   cpu_baseline  the oracle restatement on the host cores, bounded sample
   plain      the one-launch-per-pair GPU form on a sample of the same pairs
+  serve      served stream of independent jobs (continuous batching), p50/p99
+  guide_tree NJTree::generateTree on the step's own distance matrix: GPU
+             kernel (device-resident and through the C ABI) beside the oracle
 --impl reference times the reference CPU algorithm (the oracle port; the
 reference's own build is not available on the GPU host) on all host threads.
 """
@@ -37,6 +40,7 @@ for _p in (REPO, os.path.join(REPO, "cuda-clustalw_gb300")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
+FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal dense fp64 (an FMA counts 2; the join's criterion has none)
 OPS_PER_CELL = 8  # E, F via __viaddmax (2), H-gap term (1), diag add + 3-way max (2), max tracking (2), score (1)
 INT32_LANES_PER_SM = 128
 
@@ -65,6 +69,7 @@ def parse_args():
     ap.add_argument("--serve-seconds", type=float, default=12.0, help="length of the served arrival process")
     ap.add_argument("--serve-rate", type=float, default=6.0, help="served job arrival rate (jobs/s)")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--no-tree", action="store_true", help="skip the guide-tree leg")
     ap.add_argument("--autotune", action="store_true", help="pick the tiny-frame thresholds for this workload first")
     return ap.parse_args()
 
@@ -313,6 +318,93 @@ def served_leg(args, matrix, params, device):
     }
 
 
+def packed_distmatrix(n, pairs, dist):
+    """The DistMatrix elements FullPairwiseAlign leaves (SymMatrix of size n+1,
+    general/SymMatrix.h:166-197): the float distance stored as a double."""
+    el = np.zeros((n + 1) * (n + 2) // 2, dtype=np.float64)
+    si = pairs[:, 0].astype(np.int64)
+    sj = pairs[:, 1].astype(np.int64)
+    el[sj * (sj + 1) // 2 + si] = np.asarray(dist, dtype=np.float32).astype(np.float64)
+    return el
+
+
+def guide_tree_leg(args, n, pairs, dist, device, peaks):
+    """Guide tree (NJTree::generateTree, tree/NJTree.cpp:161-748) on the distance
+    matrix this step produced: the GPU join kernel device-resident (CUDA events
+    on its stream) and through the C ABI with host buffers, checked bit for bit
+    against the oracle restatement, which is also the timed CPU baseline."""
+    import torch
+
+    from clustalw_gb300.tree import NJGpu
+    from oracle import oracle
+
+    el = packed_distmatrix(n, pairs, dist)
+    nj = NJGpu(device)
+    dev = torch.device("cuda", device)
+    d_in = torch.from_numpy(el).to(dev)
+    d_out = torch.empty_like(d_in)
+    d_left = torch.empty(n + 2, dtype=torch.float64, device=dev)
+    d_right = torch.empty(n + 2, dtype=torch.float64, device=dev)
+    d_desc = torch.empty((n + 1) * (n + 1), dtype=torch.int32, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize()
+    steps, warmup = max(1, args.steps), max(3, args.warmup)
+    times = []
+    for k in range(warmup + steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        nj.tree_device(n, d_in.data_ptr(), d_out.data_ptr(), d_left.data_ptr(), d_right.data_ptr(),
+                       d_desc.data_ptr(), None, stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    pairs_eval, kernel_s = nj.last_stats()
+    dev_s = statistics.median(times)
+    # Through the C ABI with host buffers (copies in and out inside the timing).
+    e2e = []
+    for k in range(steps + 1):
+        w = el.copy()
+        t = time.perf_counter()
+        left, right, desc, _ = nj.tree(n, w)
+        if k:
+            e2e.append(time.perf_counter() - t)
+    e2e_s = statistics.median(e2e)
+    # Oracle: parity and the CPU baseline (one thread, like the reference).
+    t = time.perf_counter()
+    want = oracle.nj_tree(n, el.copy())
+    cpu_s = time.perf_counter() - t
+    same = (np.array_equal(left.view(np.int64), want[0].view(np.int64))
+            and np.array_equal(right.view(np.int64), want[1].view(np.int64))
+            and np.array_equal(desc, want[2]) and np.array_equal(w.view(np.int64), want[3].view(np.int64))
+            and np.array_equal(d_out.cpu().numpy().view(np.int64), want[3].view(np.int64)))
+    nj.close()
+    fp64_ops = 4 * pairs_eval  # fnseqs2*d + 2*sumd - diq - djq per pair (NJTree.cpp:331-376)
+    fp64_peak = FP64_NOMINAL_TFLOPS
+    return {
+        "metric": "ms per tree",
+        "value": 1e3 * dev_s,
+        "unit": "ms",
+        "higher_is_better": False,
+        "n": n,
+        "cycles": n - 3,
+        "pairs_evaluated": int(pairs_eval),
+        "e2e": {"value": 1e3 * e2e_s, "unit": "ms", "h2d_bytes_per_step": int(el.nbytes),
+                "d2h_bytes_per_step": int(el.nbytes + 16 * (n + 2) + 4 * (n + 1) * (n + 1)),
+                "call": "cwgpu_nj_tree (host DistMatrix in; branches, treeDesc, joined matrix out)"},
+        "cpu_baseline": {"value": 1e3 * cpu_s, "unit": "ms", "cores": 1, "kind": "port",
+                         "sample": f"the full tree on the same {n}-sequence matrix (NJTree is single-threaded)"},
+        "speedup_vs_cpu": cpu_s / dev_s,
+        "bit_exact_vs_oracle": bool(same),
+        "roofline": {"bound": "latency (sequential per-cycle sums and one join per cycle)",
+                     "kernel": "k_nj", "fp64_ops_per_launch": int(fp64_ops),
+                     "achieved": fp64_ops / kernel_s / 1e12, "peak": fp64_peak, "unit": "TFLOP/s (fp64 add/mul)",
+                     "frac": fp64_ops / kernel_s / 1e12 / fp64_peak,
+                     "peak_source": "nominal GB300 fp64 (no measured fp64 peak is available)"},
+        "gpu_launches": 1,
+    }
+
+
 # ---------------------------------------------------------------- GPU arm
 
 
@@ -513,6 +605,8 @@ def ours_arm(args):
             line["cpu_baseline"] = cpu_baseline(seqs, matrix, params, pairs, args.cpu_seconds)
             if not args.no_serve:
                 line["serve"] = served_leg(args, matrix, params, local)
+            if not args.no_tree:
+                line["guide_tree"] = guide_tree_leg(args, len(seqs), pairs, dist_out, local, peaks)
         print(json.dumps(line), flush=True)
     plan.close()
     ctx.close()

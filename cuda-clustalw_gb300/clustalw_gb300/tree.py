@@ -107,6 +107,44 @@ class NJGpu:
         return p.value, s.value
 
 
+# The reference's verbose report (NJTree.cpp:209-236, 413-470, 694-740):
+# C++ ostream with setprecision(5) (%g style) and setw(9) for branch lengths.
+_REPORT_HEAD = ("\n\n\t\t\tNeighbor-joining Method\n"
+                "\n Saitou, N. and Nei, M. (1987) The Neighbor-joining Method:"
+                "\n A New Method for Reconstructing Phylogenetic Trees."
+                "\n Mol. Biol. Evol., 4(4), 406-425\n\n\n This is an UNROOTED tree\n"
+                "\n Numbers in parentheses are branch lengths\n\n")
+
+
+def _br(v):
+    return "%9s" % ("%.5g" % v)
+
+
+def _side(node, index, branch):
+    return ("Node:" if node else " SEQ:") + "%4d" % index + " (" + _br(branch) + ")"
+
+
+def nj_report(n, joins, left, right):
+    """The cycle report NJTree writes when verbose, rebuilt from the joins
+    (mini, minj per cycle) and branch lengths of a tree of n > 2 sequences."""
+    out = []
+    joined = [False] * (n + 1)  # av[i] > 0 in the reference
+    gone = [False] * (n + 1)
+    for nc in range(1, n - 2):
+        mini, minj = int(joins[nc - 1][0]), int(joins[nc - 1][1])
+        out.append("\n Cycle" + "%4d" % nc + "     = " + _side(joined[mini], mini, left[nc]) + " joins "
+                   + _side(joined[minj], minj, right[nc]) + "\n")
+        joined[mini] = True
+        gone[minj] = True
+    out.append("\n Cycle" + "%4d" % (n - 2) + " (Last cycle, trichotomy):\n")
+    rest = [i for i in range(1, n + 1) if not gone[i]]
+    for k, i in enumerate(rest, start=1):
+        out.append(("\n\t\t Node:" if joined[i] else "\n\t\t  SEQ:") + "%4d" % i + " (" + _br(left[n - 3 + k]) + ") "
+                   + ("joins" if k < 3 else ""))
+    out.append("\n")
+    return "".join(out)
+
+
 class NJTree(ClusterTreeAlgorithm):
     """NJTree (tree/NJTree.h) on the GPU. As UnRootedClusterTree::treeFromDistMatrix
     calls it (tree/UnRootedClusterTree.cpp:241-246), distMat holds seqInfo.numSeqs
@@ -122,10 +160,19 @@ class NJTree(ClusterTreeAlgorithm):
         self.verbose = bool(choice)
 
     def generateTree(self, phyTree, distMat, seqInfo, tree=None):
+        """tree: a text stream for the verbose report (None: no report, as
+        the reference resets verbose when given no stream)."""
+        if tree is None:
+            self.verbose = False
         n = seqInfo.lastSeq - seqInfo.firstSeq + 1
         if n < 2:
             raise ValueError("NJTree needs at least two sequences")
+        if self.verbose:
+            tree.write(_REPORT_HEAD)
         if n == 2:  # NJTree.cpp:218-229: returns before touching the tree
+            if self.verbose:
+                d = distMat.GetAt(seqInfo.firstSeq, seqInfo.firstSeq + 1)
+                tree.write("Cycle   1     =  SEQ:   1 (" + _br(d) + ") joins  SEQ:   2 (" + _br(d) + ")")
             return
         if self._gpu is None:
             self._gpu = NJGpu(self._device)
@@ -140,3 +187,5 @@ class NJTree(ClusterTreeAlgorithm):
         phyTree.rightBranch = right
         phyTree.treeDesc = desc
         self.lastJoins = joins
+        if self.verbose:
+            tree.write(nj_report(n, joins, left, right))

@@ -16,6 +16,27 @@
 namespace clustalw
 {
 
+// One context per device for the life of the process. The reference news a
+// FullPairwiseAlign per alignment and deletes it through PairwiseAlignBase*
+// (Clustal.cpp:151-162), whose destructor is not virtual, so this class must
+// not own device resources; the cached context also keeps the device set-up
+// between calls. Released at exit. Not thread-safe, like the reference class.
+static const int kMaxDevices = 64;
+static cwgpu_context* sharedContexts[kMaxDevices];
+static bool cleanupRegistered = false;
+
+static void releaseContexts()
+{
+    for (int d = 0; d < kMaxDevices; ++d)
+    {
+        if (sharedContexts[d])
+        {
+            cwgpu_destroy(sharedContexts[d]);
+            sharedContexts[d] = 0;
+        }
+    }
+}
+
 GpuFullPairwiseAlign::GpuFullPairwiseAlign(int dev)
 : device(dev),
   ctx(0)
@@ -24,10 +45,6 @@ GpuFullPairwiseAlign::GpuFullPairwiseAlign(int dev)
 
 GpuFullPairwiseAlign::~GpuFullPairwiseAlign()
 {
-    if (ctx)
-    {
-        cwgpu_destroy(ctx);
-    }
 }
 
 static void gpuFailure(cwgpu_context* ctx, int status)
@@ -104,9 +121,20 @@ void GpuFullPairwiseAlign::pairwiseAlign(Alignment *alignPtr, DistMatrix *distMa
     }
 
     int status = CWGPU_OK;
+    if (device < 0 || device >= kMaxDevices)
+    {
+        gpuFailure(0, CWGPU_ERR_ARG);
+    }
+    ctx = sharedContexts[device];
     if (!ctx)
     {
+        if (!cleanupRegistered)
+        {
+            atexit(releaseContexts);
+            cleanupRegistered = true;
+        }
         status = cwgpu_create(device, &ctx);
+        sharedContexts[device] = ctx;
         if (status != CWGPU_OK)
         {
             gpuFailure(ctx, status);

@@ -32,7 +32,7 @@ class GpuFullPairwiseAlign : public PairwiseAlignBase
         GpuFullPairwiseAlign(const GpuFullPairwiseAlign&);
         GpuFullPairwiseAlign& operator=(const GpuFullPairwiseAlign&);
         int device;
-        cwgpu_context* ctx;
+        cwgpu_context* ctx;  // the process-wide context of this device (see the .cpp)
 };
 
 }

@@ -475,8 +475,10 @@ static size_t sym_idx(int i, int j) {
  * it. d: packed SymMatrix elements of size n+1, updated in place like the
  * reference. left/right: n+2 doubles; desc: (n+1)*(n+1) ints, row-major.
  * Valid nodes are kept in ascending order, which is the order the reference's
- * linked list visits them. Returns 0, or 1 if n < 2. */
-int cwo_nj_tree(int n, double* d, double* left, double* right, int32_t* desc) {
+ * linked list visits them. joins (may be NULL): 2*(n-3) ints, (mini, minj) of
+ * every cycle, as the verbose report names them (NJTree.cpp:413-470).
+ * Returns 0, or 1 if n < 2. */
+int cwo_nj_tree(int n, double* d, double* left, double* right, int32_t* desc, int32_t* joins) {
     if (n < 2) return 1;
     if (n == 2) return 0; /* :218-229 returns before touching the tree */
     const int W = n + 1;
@@ -537,6 +539,10 @@ int cwo_nj_tree(int n, double* d, double* left, double* right, int32_t* desc) {
         if (fabs(bj) < 0.0001) bj = 0.0;
         left[nc] = bi;
         right[nc] = bj;
+        if (joins) {
+            joins[2 * (nc - 1)] = mini;
+            joins[2 * (nc - 1) + 1] = minj;
+        }
         for (i = 1; i <= n; i++) desc[(size_t)nc * W + i] = 0;
         const int who[2] = {mini, minj}, typ[2] = {typei, typej};
         for (int side = 0; side < 2; side++) {

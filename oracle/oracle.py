@@ -83,7 +83,8 @@ def lib():
             ctypes.c_int32,
         ]
         L.cwo_nj_tree.restype = ctypes.c_int
-        L.cwo_nj_tree.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.cwo_nj_tree.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                  ctypes.c_void_p]
         L.cwo_gap_penalties.restype = None
         L.cwo_gap_penalties.argtypes = [
             ctypes.POINTER(Params),
@@ -143,27 +144,33 @@ def align_pairs(seqs, matrix, params, pairs, nthreads=None):
     return out
 
 
-def nj_tree(n, elements):
+def nj_tree(n, elements, want_joins=False):
     """NJTree::generateTree restated (oracle.c cwo_nj_tree). Returns
-    (left_branch[n+2], right_branch[n+2], tree_desc[(n+1),(n+1)], elements_after)."""
+    (left_branch[n+2], right_branch[n+2], tree_desc[(n+1),(n+1)], elements_after)
+    and, with want_joins, the (mini, minj) of every cycle as a fifth item."""
     d = np.ascontiguousarray(np.array(elements, dtype=np.float64))
     left = np.zeros(n + 2, dtype=np.float64)
     right = np.zeros(n + 2, dtype=np.float64)
     desc = np.zeros((n + 1) * (n + 1), dtype=np.int32)
-    rc = lib().cwo_nj_tree(int(n), d.ctypes.data, left.ctypes.data, right.ctypes.data, desc.ctypes.data)
+    joins = np.zeros((max(n - 3, 0) + 1, 2), dtype=np.int32)
+    rc = lib().cwo_nj_tree(int(n), d.ctypes.data, left.ctypes.data, right.ctypes.data, desc.ctypes.data,
+                           joins.ctypes.data)
     if rc != 0:
         raise RuntimeError("cwo_nj_tree failed")
-    return left, right, desc.reshape(n + 1, n + 1), d
+    out = (left, right, desc.reshape(n + 1, n + 1), d)
+    return out + (joins[: max(n - 3, 0)],) if want_joins else out
 
 
-def run_reference_nj(n, elements, workdir):
-    """Run the reference NJTree through the harness (built here only)."""
+def run_reference_nj(n, elements, workdir, report=False):
+    """Run the reference NJTree through the harness (built here only). With
+    report=True also returns the reference's verbose cycle report as text."""
     inp = os.path.join(workdir, "nj_in.bin")
     out = os.path.join(workdir, "nj_out.bin")
+    rep = os.path.join(workdir, "nj_report.txt")
     with open(inp, "wb") as f:
         f.write(np.int32(n).tobytes())
         f.write(np.asarray(elements, dtype="<f8").tobytes())
-    subprocess.run([REF_HARNESS, "--nj", inp, out], check=True, stdout=subprocess.DEVNULL)
+    subprocess.run([REF_HARNESS, "--nj", inp, out] + ([rep] if report else []), check=True, stdout=subprocess.DEVNULL)
     with open(out, "rb") as f:
         buf = f.read()
     off = 4
@@ -177,6 +184,9 @@ def run_reference_nj(n, elements, workdir):
     el = np.frombuffer(buf, "<f8", nel, off).copy()
     off += 8 * nel
     secs = float(np.frombuffer(buf, "<f8", 1, off)[0])
+    if report:
+        with open(rep) as f:
+            return left, right, desc, el, secs, f.read()
     return left, right, desc, el, secs
 
 

@@ -12,14 +12,15 @@
 // DistMatrix sized numSeqs+1, then one pairwiseAlign(iStart, iEnd, jStart, jEnd).
 //
 // Usage: refharness IN.fa OUT.bin [iStart iEnd jStart jEnd]
-//        refharness --nj IN.dist OUT.tree
+//        refharness --nj IN.dist OUT.tree [OUT.report]
 //
 // --nj runs clustalw::NJTree::generateTree (tree/NJTree.cpp:161-748) the way
 // UnRootedClusterTree::treeFromDistMatrix calls it (tree/UnRootedClusterTree.cpp:
 // 236-245): IN.dist is int32 n followed by the packed SymMatrix elements
 // (double[(n+1)(n+2)/2]); OUT.tree is int32 n, double leftBranch[n+2],
 // double rightBranch[n+2], int32 treeDesc[(n+1)*(n+1)], and the SymMatrix
-// elements as generateTree leaves them (it works in place).
+// elements as generateTree leaves them (it works in place). With OUT.report the
+// tree is built verbose and the reference's cycle report is written there.
 //
 // OUT.bin layout (little endian):
 //   char[8]  "CWREF01\0"
@@ -35,6 +36,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <fstream>
 #include <string>
 #include <vector>
 
@@ -66,7 +68,7 @@ static void put(FILE* f, const void* p, size_t n) {
     }
 }
 
-static int run_nj(const char* in, const char* out) {
+static int run_nj(const char* in, const char* out, const char* report) {
     FILE* f = fopen(in, "rb");
     if (!f) return 4;
     int n = 0;
@@ -83,8 +85,13 @@ static int run_nj(const char* in, const char* out) {
     info.lastSeq = n;
     info.numSeqs = n;
     NJTree nj;
+    std::ofstream rep;
+    if (report) {
+        rep.open(report);
+        nj.setVerbose(true);
+    }
     auto t0 = std::chrono::steady_clock::now();
-    nj.generateTree(&tree, &dist, &info);
+    nj.generateTree(&tree, &dist, &info, report ? &rep : 0);
     double secs = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     tree.leftBranch.resize(n + 2, 0.0);
     tree.rightBranch.resize(n + 2, 0.0);
@@ -102,10 +109,10 @@ static int run_nj(const char* in, const char* out) {
 }
 
 int main(int argc, char** argv) {
-    if (argc == 4 && std::string(argv[1]) == "--nj") {
+    if ((argc == 4 || argc == 5) && std::string(argv[1]) == "--nj") {
         userParameters = new UserParameters(false);
         utilityObject = new Utility();
-        return run_nj(argv[2], argv[3]);
+        return run_nj(argv[2], argv[3], argc == 5 ? argv[4] : 0);
     }
     if (argc != 3 && argc != 7) {
         fprintf(stderr, "usage: %s IN.fa OUT.bin [iStart iEnd jStart jEnd]\n", argv[0]);

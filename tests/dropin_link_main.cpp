@@ -1,7 +1,8 @@
-// Link check for the C++ drop-in: defines the reference's five process
+// Link check for the C++ drop-ins: defines the reference's five process
 // globals (as CPU/clustalw-2.0.11/src/main.cpp:23-30 does), constructs
-// GpuFullPairwiseAlign behind a PairwiseAlignBase pointer, and exits without
-// calling it (this binary is built and linked on a host without a GPU).
+// GpuFullPairwiseAlign behind a PairwiseAlignBase pointer and GpuNJTree behind
+// a ClusterTreeAlgorithm pointer, and exits without calling them (this binary
+// is built and linked on a host without a GPU).
 #include "pairwise/PairwiseAlignBase.h"
 #include "general/DebugLog.h"
 #include "general/Stats.h"
@@ -9,6 +10,7 @@
 #include "general/Utility.h"
 #include "substitutionMatrix/SubMatrix.h"
 #include "GpuFullPairwiseAlign.h"
+#include "GpuNJTree.h"
 
 namespace clustalw {
 UserParameters* userParameters;
@@ -21,5 +23,10 @@ Stats* statsObject;
 int main() {
     clustalw::PairwiseAlignBase* p = new clustalw::GpuFullPairwiseAlign(0);
     delete p;
+    // Deleted through the base pointer, as UnRootedClusterTree.cpp:248 does;
+    // the drop-ins own no per-object device resources.
+    clustalw::ClusterTreeAlgorithm* t = new clustalw::GpuNJTree(0);
+    t->setVerbose(false);
+    delete t;
     return 0;
 }

@@ -59,10 +59,12 @@ def run_fasta(text, name, rng=None):
 
 
 def save_nj(name, n, elements):
+    """NJ fixture: inputs, the reference's tree and joined matrix, and its
+    verbose cycle report (NJTree.cpp:209-236, 413-470, 694-740)."""
     with tempfile.TemporaryDirectory() as d:
-        left, right, desc, el, secs = O.run_reference_nj(n, elements, d)
+        left, right, desc, el, secs, report = O.run_reference_nj(n, elements, d, report=True)
     np.savez_compressed(os.path.join(OUT, name + ".npz"), n=np.int32(n), elements=np.asarray(elements, np.float64),
-                        left=left, right=right, desc=desc, elements_after=el)
+                        left=left, right=right, desc=desc, elements_after=el, report=np.array(report))
     print(f"{name}: NJ on {n} sequences, ref {secs:.4f}s")
 
 

@@ -43,13 +43,14 @@ def random_matrix(n, seed, ties=False):
 
 
 def check(nj, oracle_mod, n, el):
-    want = oracle_mod.nj_tree(n, el.copy())
+    want = oracle_mod.nj_tree(n, el.copy(), want_joins=True)
     got_el = el.copy()
     left, right, desc, joins = nj.tree(n, got_el, want_joins=True)
     assert same_bits(left, want[0])
     assert same_bits(right, want[1])
     assert np.array_equal(desc, want[2])
     assert same_bits(got_el, want[3])
+    assert np.array_equal(joins, want[4])
     return joins
 
 
@@ -106,6 +107,26 @@ def test_gpu_nj_first_join_is_first_minimum(nj):
                 best, arg = t, (ii, jj)
     _, _, _, joins = nj.tree(n, el.copy(), want_joins=True)
     assert tuple(joins[0]) == arg
+
+
+@pytest.mark.parametrize("name", ["nj_fixture_100_97", "nj_ties_30", "nj_random_4"])
+def test_gpu_nj_verbose_report_matches_reference(nj, name):
+    """NJTree.generateTree with a report stream writes the reference's own
+    verbose report (NJTree.cpp:209-236, 413-470, 694-740)."""
+    import io
+
+    from clustalw_gb300.pairwise import DistMatrix
+    from clustalw_gb300.tree import NJTree, PhyloTree, SeqInfo
+
+    g = load_nj_golden(name)
+    n = int(g["n"])
+    dm = DistMatrix(n + 1)
+    dm.getElements()[:] = g["elements"]
+    algo = NJTree(gpu=nj)
+    algo.setVerbose(True)
+    out = io.StringIO()
+    algo.generateTree(PhyloTree(), dm, SeqInfo(1, n, n), out)
+    assert out.getvalue() == str(g["report"])
 
 
 def test_gpu_nj_two_sequences_untouched(nj):

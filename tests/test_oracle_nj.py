@@ -40,3 +40,15 @@ def test_nj_golden_has_ties():
     s = sum(d(i, j) for j in range(1, n + 1) for i in range(1, j))
     tot = [(n - 2) * d(i, j) + 2 * s - r[i] - r[j] for j in range(2, n + 1) for i in range(1, j)]
     assert sum(1 for t in tot if t == min(tot)) > 1
+
+
+@pytest.mark.parametrize("name", nj_golden_names())
+def test_nj_report_matches_reference(name, oracle_mod):
+    """The verbose cycle report the host mirror writes (from the joins and
+    branch lengths) is the reference's own report, character for character."""
+    from clustalw_gb300.tree import _REPORT_HEAD, nj_report
+
+    g = load_nj_golden(name)
+    n = int(g["n"])
+    left, right, _, _, joins = oracle_mod.nj_tree(n, g["elements"], want_joins=True)
+    assert _REPORT_HEAD + nj_report(n, joins, left, right) == str(g["report"])
