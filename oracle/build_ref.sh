@@ -20,7 +20,7 @@ mkdir -p "$OUT/obj" "$OUT/include"
 printf '#define CLUSTALW_NAME "ClustalW"\n#define CLUSTALW_VERSION "2.0.11"\n' > "$OUT/include/clustalw_version.h"
 CXX=${CXX:-g++}
 FLAGS="-O2 -std=gnu++98 -w -DOS_UNIX=1 -I$SRC -I$OUT/include"
-UNITS="pairwise/FullPairwiseAlign substitutionMatrix/SubMatrix general/UserParameters
+UNITS="pairwise/FullPairwiseAlign pairwise/FastPairwiseAlign substitutionMatrix/SubMatrix general/UserParameters
 general/Utility alignment/Alignment alignment/Sequence general/SymMatrix
 general/VectorOutOfRange general/InvalidCombination general/DebugLog general/Stats
 general/ClustalWResources general/OutputFile fileInput/FileReader fileInput/FileParser

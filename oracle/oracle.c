@@ -642,3 +642,348 @@ int cwo_nj_tree(int n, double* d, double* left, double* right, int32_t* desc, in
     free(valid);
     return 0;
 }
+
+/* ------------------------------------------------- k-tuple quick distances */
+
+/* The userParameters values FastPairwiseAlign::pairAlign reads
+ * (pairwise/FastPairwiseAlign.cpp:176-183), after setDNAParams/setProtParams. */
+typedef struct cwo_fast_params {
+    int32_t dna, ktup, window, window_gap, signif, percent, max_aa, max_aln_length;
+} cwo_fast_params;
+
+typedef struct cwo_fast_result {
+    double dist;       /* (100 - calcScore) / 100, as SetAt stores it */
+    int32_t score;     /* accum[0][maxSoFar], 0 if no fragment */
+    int32_t frags;     /* fragments made (currFrag) */
+    int32_t partial;   /* the "(Partial alignment)" cut-off was hit */
+    int32_t pad;
+} cwo_fast_result;
+
+typedef struct fast_scratch {
+    int *displ, *slopes, *diag, *zza, *zzb, *zzc, *zzd, *acc[5];
+} fast_scratch;
+
+/* FastPairwiseAlign.cpp:163-164: A C G T U -> 0 1 2 3 3, anything else -1. */
+static int aa2dna(int code) {
+    switch (code) {
+        case 0: return 0;
+        case 2: return 1;
+        case 6: return 2;
+        case 18: case 19: return 3;
+        default: return -1;
+    }
+}
+
+/* makePPtrs / makeNPtrs (FastPairwiseAlign.cpp:406-510): pl[code] = last
+ * position of each k-tuple code, tptr[i] = previous position with the same
+ * code (0 ends the chain). seq is 0-based here, positions 1-based. */
+static void make_ptrs(const cwo_fast_params* P, int* tptr, int* pl, const int8_t* seq, int length) {
+    const int base = P->dna ? 4 : P->max_aa + 1;
+    int limit = 1, a[10], i, j;
+    a[1] = 1;
+    for (i = 2; i <= P->ktup; i++) a[i] = a[i - 1] * base;
+    for (i = 1; i <= P->ktup; i++) limit *= base;
+    for (i = 1; i <= limit; ++i) pl[i] = 0;
+    for (i = 1; i <= length; ++i) tptr[i] = 0;
+    for (i = 1; i <= length - P->ktup + 1; ++i) {
+        int code = 0, bad = 0;
+        for (j = 1; j <= P->ktup; ++j) {
+            int r = seq[i + j - 2];
+            if (P->dna) {
+                r = (r >= 0 && r < 36) ? aa2dna(r) : -1;
+                if (r < 0 || r > 3) { bad = 1; break; }
+            } else if (r < 0 || r > P->max_aa) {
+                bad = 1;
+                break;
+            }
+            code += r * a[j];
+        }
+        if (bad) continue;
+        ++code;
+        if (pl[code] != 0) tptr[i] = pl[code];
+        pl[code] = i;
+    }
+}
+
+/* desQuickSort (FastPairwiseAlign.cpp:585-658): the reference's quicksort of
+ * array1[1 .. size-1] ascending, array2 permuted alongside. Element `size`
+ * itself is not part of the sort. */
+static void des_quick_sort(int* array1, int* array2, int size) {
+    int lst[50], ust[50], p = 1, i, j, t;
+    lst[1] = 1;
+    ust[1] = size - 1;
+    while (p > 0) {
+        if (lst[p] >= ust[p]) {
+            p--;
+        } else {
+            i = lst[p] - 1;
+            j = ust[p];
+            int piv = array1[j];
+            while (i < j) {
+                for (i = i + 1; array1[i] < piv; i++)
+                    ;
+                for (j = j - 1; j > i; j--)
+                    if (array1[j] <= piv) break;
+                if (i < j) {
+                    t = array1[i]; array1[i] = array1[j]; array1[j] = t;
+                    t = array2[i]; array2[i] = array2[j]; array2[j] = t;
+                }
+            }
+            j = ust[p];
+            t = array1[i]; array1[i] = array1[j]; array1[j] = t;
+            t = array2[i]; array2[i] = array2[j]; array2[j] = t;
+            if (i - lst[p] < ust[p] - i) {
+                lst[p + 1] = lst[p];
+                ust[p + 1] = i - 1;
+                lst[p] = i + 1;
+            } else {
+                lst[p + 1] = i + 1;
+                ust[p + 1] = ust[p];
+                ust[p] = i - 1;
+            }
+            p = p + 1;
+        }
+    }
+}
+
+/* fragRelPos (FastPairwiseAlign.cpp:563-583). */
+static int frag_rel_pos(int a1, int b1, int a2, int b2, int ktup) {
+    if (a1 - b1 == a2 - b2) return a2 < a1;
+    return a2 + ktup - 1 < a1 && b2 + ktup - 1 < b1;
+}
+
+/* putFrag (FastPairwiseAlign.cpp:524-561): fragments kept in a list sorted by
+ * score, accum[4] the links, maxSoFar the head. */
+static void put_frag(int** acc, int* maxSoFar, int currFrag, int fs, int v1, int v2, int flen) {
+    acc[0][currFrag] = fs;
+    acc[1][currFrag] = v1;
+    acc[2][currFrag] = v2;
+    acc[3][currFrag] = flen;
+    if (!*maxSoFar) {
+        *maxSoFar = 1;
+        acc[4][currFrag] = 0;
+        return;
+    }
+    if (fs >= acc[0][*maxSoFar]) {
+        acc[4][currFrag] = *maxSoFar;
+        *maxSoFar = currFrag;
+        return;
+    }
+    int next = *maxSoFar, end;
+    while (1) {
+        end = next;
+        next = acc[4][next];
+        if (fs >= acc[0][next]) break;
+    }
+    acc[4][currFrag] = next;
+    acc[4][end] = currFrag;
+}
+
+/* pairAlign (FastPairwiseAlign.cpp:168-400) for sequence 1 (already in
+ * zza/zzc) against sequence 2 (zzb/zzd). */
+static void pair_align(const cwo_fast_params* P, fast_scratch* S, const int8_t* seq, int l1, int l2,
+                       cwo_fast_result* R) {
+    const int ktup = P->ktup;
+    const int base = P->dna ? 4 : P->max_aa + 1;
+    int pot[10], limit = 1, i, j;
+    pot[1] = 1;
+    for (i = 2; i <= ktup; i++) pot[i] = pot[i - 1] * base;
+    for (i = 1; i <= ktup; i++) limit *= base;
+    int* displ = S->displ;
+    int* slopes = S->slopes;
+    int* diag = S->diag;
+    int** acc = S->acc;
+    const int tl1 = (l1 + l2) - 1;
+    for (i = 1; i <= tl1; ++i) {
+        slopes[i] = displ[i] = 0;
+        diag[i] = i;
+    }
+    /* diagonal hit counts */
+    for (i = 1; i <= limit; ++i) {
+        int vn1 = S->zzc[i];
+        while (vn1) {
+            int vn2 = S->zzd[i];
+            while (vn2 != 0) {
+                ++displ[vn1 - vn2 + l2];
+                vn2 = S->zzb[vn2];
+            }
+            vn1 = S->zza[vn1];
+        }
+    }
+    des_quick_sort(displ, diag, tl1);
+    j = tl1 - P->signif + 1;
+    if (j < 1) j = 1;
+    for (i = tl1; i >= j; i--)
+        if (displ[i] > 0) {
+            int pos = diag[i];
+            int l = (1 > pos - P->window) ? 1 : pos - P->window;
+            int m = (tl1 < pos + P->window) ? tl1 : pos + P->window;
+            for (; l <= m; l++) slopes[l] = 1;
+        }
+    for (i = 1; i <= tl1; i++) displ[i] = 0;
+    int currFrag = 0, maxSoFar = 0, next = 0;
+    R->partial = 0;
+    for (i = 1; i <= (l1 - ktup + 1); ++i) {
+        int encrypt = 0, bad = 0;
+        for (j = 1; j <= ktup; ++j) {
+            int r = seq[i + j - 2];
+            if (P->dna) {
+                r = (r >= 0 && r < 36) ? aa2dna(r) : -1;
+                if (r < 0 || r > 3) { bad = 1; break; }
+            } else if (r < 0 || r > P->max_aa) {
+                bad = 1;
+                break;
+            }
+            encrypt += r * pot[j];
+        }
+        if (bad) continue;
+        ++encrypt;
+        int vn2 = S->zzd[encrypt];
+        while (vn2) {
+            int osptr = i - vn2 + l2;
+            if (slopes[osptr] != 1) {
+                vn2 = S->zzb[vn2];
+                continue;
+            }
+            int flen = 0, fs = ktup;
+            next = maxSoFar;
+            /* the A-loop */
+            while (1) {
+                if (!next) {
+                    ++currFrag;
+                    if (currFrag >= 2 * P->max_aln_length) {
+                        R->partial = 1;
+                        goto done;
+                    }
+                    displ[osptr] = currFrag;
+                    put_frag(acc, &maxSoFar, currFrag, fs, i, vn2, flen);
+                } else {
+                    int tv1 = acc[1][next], tv2 = acc[2][next];
+                    if (frag_rel_pos(i, vn2, tv1, tv2, ktup)) {
+                        if (i - vn2 == acc[1][next] - acc[2][next]) {
+                            if (i > acc[1][next] + (ktup - 1)) {
+                                fs = acc[0][next] + ktup;
+                            } else {
+                                fs = acc[0][next] + (i - acc[1][next]);
+                            }
+                            flen = next;
+                            next = 0;
+                            continue;
+                        } else {
+                            int subt1, subt2;
+                            if (displ[osptr] == 0) {
+                                subt1 = ktup;
+                            } else if (i > acc[1][displ[osptr]] + (ktup - 1)) {
+                                subt1 = acc[0][displ[osptr]] + ktup;
+                            } else {
+                                subt1 = acc[0][displ[osptr]] + (i - acc[1][displ[osptr]]);
+                            }
+                            subt2 = acc[0][next] - P->window_gap + ktup;
+                            if (subt2 > subt1) {
+                                flen = next;
+                                fs = subt2;
+                            } else {
+                                flen = displ[osptr];
+                                fs = subt1;
+                            }
+                            next = 0;
+                            continue;
+                        }
+                    } else {
+                        next = acc[4][next];
+                        continue;
+                    }
+                }
+                break;
+            }
+            vn2 = S->zzb[vn2];
+        }
+    }
+done:
+    R->frags = currFrag;
+    R->score = maxSoFar ? acc[0][maxSoFar] : 0;
+    {
+        /* FastPairwiseAlign.cpp:88-103, in double */
+        double calc = 0.0;
+        if (maxSoFar) {
+            calc = (double)acc[0][maxSoFar];
+            if (P->percent) {
+                int dsr = l1 < l2 ? l1 : l2;
+                calc = (calc / (double)dsr) * 100.0;
+            }
+        }
+        R->dist = (100.0 - calc) / 100.0;
+    }
+}
+
+typedef struct fast_job {
+    const int8_t* codes;
+    const int64_t* offsets;
+    const int32_t* lens;
+    const cwo_fast_params* P;
+    const int32_t* pairs;
+    int64_t npairs;
+    cwo_fast_result* out;
+    int64_t next;
+    pthread_mutex_t mu;
+    int lmax;
+} fast_job;
+
+static void* fast_worker(void* arg) {
+    fast_job* J = (fast_job*)arg;
+    const cwo_fast_params* P = J->P;
+    const int base = P->dna ? 4 : P->max_aa + 1;
+    int limit = 1, k;
+    for (k = 0; k < P->ktup; k++) limit *= base;
+    const int nd = 2 * J->lmax + 2, na = 2 * P->max_aln_length + 2;
+    fast_scratch S;
+    S.displ = (int*)calloc(nd, sizeof(int));
+    S.slopes = (int*)calloc(nd, sizeof(int));
+    S.diag = (int*)calloc(nd, sizeof(int));
+    S.zza = (int*)calloc(J->lmax + 2, sizeof(int));
+    S.zzb = (int*)calloc(J->lmax + 2, sizeof(int));
+    S.zzc = (int*)calloc(limit + 2, sizeof(int));
+    S.zzd = (int*)calloc(limit + 2, sizeof(int));
+    for (k = 0; k < 5; k++) S.acc[k] = (int*)calloc(na, sizeof(int));
+    while (1) {
+        pthread_mutex_lock(&J->mu);
+        int64_t q = J->next;
+        J->next += 16;
+        pthread_mutex_unlock(&J->mu);
+        if (q >= J->npairs) break;
+        int64_t qe = q + 16 < J->npairs ? q + 16 : J->npairs;
+        for (; q < qe; ++q) {
+            const int si = J->pairs[2 * q], sj = J->pairs[2 * q + 1];
+            const int8_t* s1 = J->codes + J->offsets[si];
+            const int8_t* s2 = J->codes + J->offsets[sj];
+            make_ptrs(P, S.zza, S.zzc, s1, J->lens[si]);
+            make_ptrs(P, S.zzb, S.zzd, s2, J->lens[sj]);
+            pair_align(P, &S, s1, J->lens[si], J->lens[sj], &J->out[q]);
+        }
+    }
+    free(S.displ); free(S.slopes); free(S.diag); free(S.zza); free(S.zzb); free(S.zzc); free(S.zzd);
+    for (k = 0; k < 5; k++) free(S.acc[k]);
+    return 0;
+}
+
+/* FastPairwiseAlign::pairwiseAlign over a pair list (0-based si < sj); each
+ * pair's result is independent of the others (the reference resets its
+ * per-pair state in makePPtrs/makeNPtrs/pairAlign). */
+int cwo_fast_pairs(const int8_t* codes, const int64_t* offsets, const int32_t* lens, int32_t nseqs,
+                   const cwo_fast_params* P, const int32_t* pairs, int64_t npairs, cwo_fast_result* out,
+                   int32_t nthreads) {
+    if (P->ktup < 1 || P->ktup > 8) return 1;
+    fast_job J;
+    int k;
+    J.codes = codes; J.offsets = offsets; J.lens = lens; J.P = P; J.pairs = pairs; J.npairs = npairs;
+    J.out = out; J.next = 0; J.lmax = 1;
+    for (k = 0; k < nseqs; k++) if (lens[k] > J.lmax) J.lmax = lens[k];
+    pthread_mutex_init(&J.mu, 0);
+    if (nthreads < 1) nthreads = 1;
+    pthread_t th[256];
+    if (nthreads > 256) nthreads = 256;
+    for (k = 0; k < nthreads; k++) pthread_create(&th[k], 0, fast_worker, &J);
+    for (k = 0; k < nthreads; k++) pthread_join(th[k], 0);
+    pthread_mutex_destroy(&J.mu);
+    return 0;
+}

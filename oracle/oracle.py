@@ -85,6 +85,10 @@ def lib():
         L.cwo_nj_tree.restype = ctypes.c_int
         L.cwo_nj_tree.argtypes = [ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                   ctypes.c_void_p]
+        L.cwo_fast_pairs.restype = ctypes.c_int
+        L.cwo_fast_pairs.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int32,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                                     ctypes.c_int32]
         L.cwo_gap_penalties.restype = None
         L.cwo_gap_penalties.argtypes = [
             ctypes.POINTER(Params),
@@ -141,6 +145,31 @@ def align_pairs(seqs, matrix, params, pairs, nthreads=None):
     )
     if rc != 0:
         raise RuntimeError(f"cwo_align_pairs failed with {rc}")
+    return out
+
+
+FAST_RESULT_DTYPE = np.dtype([("dist", "<f8"), ("score", "<i4"), ("frags", "<i4"), ("partial", "<i4"), ("pad", "<i4")])
+assert FAST_RESULT_DTYPE.itemsize == 24
+
+
+class FastParams(ctypes.Structure):
+    """Mirror of cwo_fast_params: what FastPairwiseAlign::pairAlign reads."""
+
+    _fields_ = [(k, ctypes.c_int32) for k in
+                ("dna", "ktup", "window", "window_gap", "signif", "percent", "max_aa", "max_aln_length")]
+
+
+def fast_pairs(seqs, fparams, pairs, nthreads=None):
+    """k-tuple quick distances (oracle.c cwo_fast_pairs) for pairs [P, 2] of
+    0-based (si, sj); returns a structured array of FAST_RESULT_DTYPE."""
+    codes, offsets, lens = pack_sequences(seqs)
+    pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+    out = np.zeros(len(pr), dtype=FAST_RESULT_DTYPE)
+    p = FastParams(*[int(fparams[k]) for k, _ in FastParams._fields_])
+    rc = lib().cwo_fast_pairs(codes.ctypes.data, offsets.ctypes.data, lens.ctypes.data, len(seqs), ctypes.byref(p),
+                              pr.ctypes.data, len(pr), out.ctypes.data, int(nthreads or os.cpu_count() or 1))
+    if rc != 0:
+        raise RuntimeError(f"cwo_fast_pairs failed with {rc}")
     return out
 
 
@@ -219,13 +248,20 @@ def read_ref_output(path):
     """Parse the binary written by oracle/ref_harness.cpp."""
     with open(path, "rb") as f:
         buf = f.read()
-    assert buf[:8] == b"CWREF01\0", "bad magic"
+    assert buf[:8] in (b"CWREF01\0", b"CWREF02\0"), "bad magic"
+    fast = buf[:8] == b"CWREF02\0"
     off = 8
     hdr = np.frombuffer(buf, dtype="<i4", count=7, offset=off)
     off += 28
     n, dna, int_scale, mat_avg, gp1, gp2, max_aln = (int(x) for x in hdr)
     fl = np.frombuffer(buf, dtype="<f4", count=4, offset=off)
     off += 16
+    fast_params = None
+    if fast:
+        kp = np.frombuffer(buf, dtype="<i4", count=6, offset=off)
+        off += 24
+        fast_params = dict(dna=dna, ktup=int(kp[0]), window=int(kp[1]), window_gap=int(kp[2]), signif=int(kp[3]),
+                           percent=int(kp[4]), max_aa=int(kp[5]), max_aln_length=max_aln)
     matrix = np.frombuffer(buf, dtype="<i4", count=NUMRES * NUMRES, offset=off).reshape(NUMRES, NUMRES).copy()
     off += 4 * NUMRES * NUMRES
     lens = np.frombuffer(buf, dtype="<i4", count=n, offset=off).copy()
@@ -260,14 +296,16 @@ def read_ref_output(path):
         elements=elements,
         seconds=secs,
         max_aln_length=max_aln,
+        fast_params=fast_params,
     )
 
 
-def run_reference(fasta, out_bin, rng=None):
-    """Run the reference harness (needs oracle/_ref/refharness, built here only)."""
+def run_reference(fasta, out_bin, rng=None, fast=False):
+    """Run the reference harness (needs oracle/_ref/refharness, built here only);
+    fast=True runs FastPairwiseAlign instead of FullPairwiseAlign."""
     if not os.path.exists(REF_HARNESS):
         raise FileNotFoundError(REF_HARNESS)
-    cmd = [REF_HARNESS, fasta, out_bin]
+    cmd = [REF_HARNESS] + (["--fast"] if fast else []) + [fasta, out_bin]
     if rng is not None:
         cmd += [str(int(x)) for x in rng]
     subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)

@@ -12,7 +12,13 @@
 // DistMatrix sized numSeqs+1, then one pairwiseAlign(iStart, iEnd, jStart, jEnd).
 //
 // Usage: refharness IN.fa OUT.bin [iStart iEnd jStart jEnd]
+//        refharness --fast IN.fa OUT.bin [iStart iEnd jStart jEnd]
 //        refharness --nj IN.dist OUT.tree [OUT.report]
+//
+// --fast runs clustalw::FastPairwiseAlign::pairwiseAlign (the k-tuple quick
+// distances, pairwise/FastPairwiseAlign.cpp:20-139) instead; its OUT.bin starts
+// with "CWREF02\0" and adds, after the four floats, int32 ktup, window,
+// windowGap, signif, percent, maxAA (the userParameters values the call used).
 //
 // --nj runs clustalw::NJTree::generateTree (tree/NJTree.cpp:161-748) the way
 // UnRootedClusterTree::treeFromDistMatrix calls it (tree/UnRootedClusterTree.cpp:
@@ -47,6 +53,7 @@
 #include "general/UserParameters.h"
 #include "general/Utility.h"
 #include "general/clustalw.h"
+#include "pairwise/FastPairwiseAlign.h"
 #include "pairwise/FullPairwiseAlign.h"
 #include "substitutionMatrix/SubMatrix.h"
 #include "tree/NJTree.h"
@@ -109,6 +116,12 @@ static int run_nj(const char* in, const char* out, const char* report) {
 }
 
 int main(int argc, char** argv) {
+    bool fast = false;
+    if (argc > 1 && std::string(argv[1]) == "--fast") {
+        fast = true;
+        --argc;
+        ++argv;
+    }
     if ((argc == 4 || argc == 5) && std::string(argv[1]) == "--nj") {
         userParameters = new UserParameters(false);
         utilityObject = new Utility();
@@ -145,9 +158,14 @@ int main(int argc, char** argv) {
     SymMatrix dist;
     dist.ResizeRect(n + 1);
 
-    FullPairwiseAlign fpa;
     auto t0 = std::chrono::steady_clock::now();
-    fpa.pairwiseAlign(&aln, &dist, range[0], range[1], range[2], range[3]);
+    if (fast) {
+        FastPairwiseAlign qpa;
+        qpa.pairwiseAlign(&aln, &dist, range[0], range[1], range[2], range[3]);
+    } else {
+        FullPairwiseAlign fpa;
+        fpa.pairwiseAlign(&aln, &dist, range[0], range[1], range[2], range[3]);
+    }
     auto t1 = std::chrono::steady_clock::now();
     double secs = std::chrono::duration<double>(t1 - t0).count();
 
@@ -161,7 +179,7 @@ int main(int argc, char** argv) {
         fprintf(stderr, "refharness: cannot open %s\n", argv[2]);
         return 4;
     }
-    put(f, "CWREF01\0", 8);
+    put(f, fast ? "CWREF02\0" : "CWREF01\0", 8);
     int hdr[7] = {n,
                   userParameters->getDNAFlag() ? 1 : 0,
                   scale.intScale,
@@ -173,6 +191,11 @@ int main(int argc, char** argv) {
     float fl[4] = {userParameters->getPWGapOpen(), userParameters->getPWGapExtend(),
                    scale.gapOpenScale, scale.gapExtendScale};
     put(f, fl, sizeof(fl));
+    if (fast) {
+        int kp[6] = {userParameters->getKtup(), userParameters->getWindow(), userParameters->getWindowGap(),
+                     userParameters->getSignif(), userParameters->getPercent() ? 1 : 0, userParameters->getMaxAA()};
+        put(f, kp, sizeof(kp));
+    }
     put(f, matrix, sizeof(matrix));
     std::vector<int> lens(n);
     for (int s = 0; s < n; ++s) lens[s] = aln.getSeqLength(s + 1);
@@ -184,6 +207,6 @@ int main(int argc, char** argv) {
     put(f, dist.getElements(), sizeof(double) * nel);
     put(f, &secs, sizeof(secs));
     fclose(f);
-    printf("refharness: %d seqs, dna=%d, pairwise %.6f s\n", n, hdr[1], secs);
+    printf("refharness: %d seqs, dna=%d, %s pairwise %.6f s\n", n, hdr[1], fast ? "fast" : "full", secs);
     return 0;
 }

@@ -45,8 +45,28 @@ def load_golden(name):
 
 
 def golden_names():
-    """Distance-stage fixtures (the guide-tree fixtures start with nj_)."""
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz") and not f.startswith("nj_"))
+    """Full-pairwise fixtures (guide-tree fixtures start with nj_, quick
+    k-tuple fixtures with fast_)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_")))
+
+
+FAST_KEYS = ("dna", "ktup", "window", "window_gap", "signif", "percent", "max_aa", "max_aln_length")
+
+
+def fast_golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("fast_") and f.endswith(".npz"))
+
+
+def load_fast_golden(name):
+    """A quick-distance fixture: FastPairwiseAlign::pairwiseAlign of the reference
+    (pairwise/FastPairwiseAlign.cpp:20-139) on the stored sequences."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    lens = z["lens"]
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64) if len(lens) else np.zeros(0, np.int64)
+    seqs = [z["codes"][o : o + L].astype(np.int8) for o, L in zip(offs, lens)]
+    fp = dict(zip(FAST_KEYS, (int(v) for v in z["fast_params"])))
+    return dict(name=name, seqs=seqs, fast_params=fp, range=[int(v) for v in z["range"]], elements=z["elements"])
 
 
 def nj_golden_names():

@@ -58,6 +58,58 @@ def run_fasta(text, name, rng=None):
         return O.run_reference(fa, os.path.join(d, "out.bin"), rng)
 
 
+def save_fast(name, ref):
+    """k-tuple quick distances (FastPairwiseAlign) fixture: the sequences as
+    the reference's reader encoded them, the userParameters values the call
+    used, the range and the reference's DistMatrix."""
+    seqs = ref["seqs"]
+    lens = np.array([len(s) for s in seqs], dtype=np.int32)
+    codes = np.concatenate(seqs).astype(np.int8) if len(seqs) else np.zeros(0, np.int8)
+    fp = ref["fast_params"]
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), codes=codes, lens=lens,
+                        fast_params=np.array([fp[k] for k in FAST_KEYS], np.int32),
+                        range=ref["range"].astype(np.int32), elements=ref["elements"])
+    print(f"{name}: {ref['n']} seqs, range {list(ref['range'])}, ref {ref['seconds']:.2f}s")
+
+
+FAST_KEYS = ("dna", "ktup", "window", "window_gap", "signif", "percent", "max_aa", "max_aln_length")
+
+
+def make_fast():
+    """Quick (k-tuple) distances of the reference fixtures, a partial range,
+    synthetic sets and the edge-case set."""
+    with tempfile.TemporaryDirectory() as d:
+        for fx in ["100_97", "100_498", "100_1002", "100_1523"]:
+            save_fast("fast_" + fx, O.run_reference(os.path.join(FIXTURES, fx + ".fa"), os.path.join(d, "o.bin"),
+                                                    fast=True))
+        save_fast("fast_100_97_block", O.run_reference(os.path.join(FIXTURES, "100_97.fa"), os.path.join(d, "o.bin"),
+                                                       (20, 60, 40, 70), fast=True))
+    for name, text in fast_sets():
+        with tempfile.TemporaryDirectory() as d:
+            fa = os.path.join(d, "s.fa")
+            with open(fa, "w") as f:
+                f.write(text)
+            save_fast("fast_" + name, O.run_reference(fa, os.path.join(d, "o.bin"), fast=True))
+
+
+def fast_sets():
+    uneven = []
+    for f, L in enumerate([5, 30, 170, 600]):
+        uneven += synth.protein_family(10, L, 100 + f)
+    edge = ["W", "MA", "MKTAYIAKQRQISFVKSHFSRQ", "MKTAYIAKQRQISFVKSHFSRQ", "AAAAAAAAAAAAAAAAAAAA",
+            "AAAAAAAAAAGAAAAAAAAA", "MK--LVAG-HHW", "----", "XXXXBZBZXX", "GGGGGGGG", "KR",
+            "ACDEFGHIKLMNPQRSTVWY" * 12, "WWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWWW", "MSLLTEVETPTRNGWECKCSDSSD", "P"]
+    dna_edge = ["A", "AC", "ACGT" * 30, "ACGT" * 30, "AAAAAAAAAAAAAAAAAAAAAAAA", "ACGTNNNNACGT", "ACGU" * 10,
+                "GATTACA" * 9, "TTTTTTTTTTGTTTTTTTTT", "CCGG"]
+    return [
+        ("synth_protein_60x97", synth.to_fasta(synth.protein_family(60, 97, 11))),
+        ("synth_dna_40x300", synth.to_fasta(synth.dna_family(40, 300, 12))),
+        ("synth_uneven_40", synth.to_fasta(uneven)),
+        ("edge_protein", "".join(f">e{i}\n{x}\n" for i, x in enumerate(edge))),
+        ("edge_dna", "".join(f">d{i}\n{x}\n" for i, x in enumerate(dna_edge))),
+    ]
+
+
 def save_nj(name, n, elements):
     """NJ fixture: inputs, the reference's tree and joined matrix, and its
     verbose cycle report (NJTree.cpp:209-236, 413-470, 694-740)."""
@@ -144,6 +196,7 @@ def main():
     save("edge_protein", run_fasta(text, "e"))
 
     make_nj()
+    make_fast()
 
     os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
     with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
@@ -155,5 +208,8 @@ if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "--nj-only":
         O.build()
         make_nj()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--fast-only":
+        O.build()
+        make_fast()
     else:
         main()
