@@ -14,8 +14,8 @@ INCLUDE = os.path.join(REPO_ROOT, "include")
 LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcwgpu.so")
 
-SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu", "cwgpu_serve.cu", "cwgpu_nj.cu"]
-HEADERS = ["cwgpu_device.cuh"]
+SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu", "cwgpu_serve.cu", "cwgpu_nj.cu", "cwgpu_fast.cu"]
+HEADERS = ["cwgpu_device.cuh", "cwgpu_context.h"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -71,6 +71,28 @@ PAIR_STATS_DTYPE = np.dtype(
     ]
 )
 
+class FastParams(ctypes.Structure):
+    """cwgpu_fast_params: what FastPairwiseAlign::pairAlign reads from userParameters."""
+
+    _fields_ = [(k, ctypes.c_int32) for k in
+                ("dna", "ktup", "window", "window_gap", "signif", "percent", "max_aa", "max_aln_length")]
+
+    @classmethod
+    def from_dict(cls, d):
+        return cls(*[int(d.get(k, 0)) for k, _ in cls._fields_])
+
+    @classmethod
+    def defaults(cls, dna, max_aln_length=0):
+        """The reference's defaults after setDNAParams/setProtParams
+        (UserParameters.cpp:86-94, 133)."""
+        if dna:
+            return cls(1, 2, 4, 5, 4, 1, 24, max_aln_length)
+        return cls(0, 1, 5, 3, 5, 1, 24, max_aln_length)
+
+
+FAST_STATS_DTYPE = np.dtype([("score", "<i4"), ("frags", "<i4"), ("partial", "<i4"), ("pad", "<i4")])
+
+
 class Tuning(ctypes.Structure):
     """cwgpu_tuning: tiny-frame thresholds of the Myers-Miller stage."""
 
@@ -143,6 +165,15 @@ SIGNATURES = {
     "cwgpu_align_pairs_noalloc": (
         ctypes.c_int,
         [_vp, _vp, _vp, _i32, _i32, _vp, ctypes.POINTER(Params), _vp, _i64, _vp, _vp, _vp],
+    ),
+    "cwgpu_fast_pairwise_align": (
+        ctypes.c_int,
+        [_vp, ctypes.POINTER(FastParams), _i32, _i32, _i32, _i32, _vp, _i32, _vp],
+    ),
+    "cwgpu_fast_align_pairs": (ctypes.c_int, [_vp, ctypes.POINTER(FastParams), _vp, _i64, _vp, _vp]),
+    "cwgpu_fast_align_pairs_device": (
+        ctypes.c_int,
+        [_vp, ctypes.POINTER(FastParams), _vp, _vp, _i64, _vp, _vp, _vp],
     ),
     # include/cwgpu_nj.h
     "cwgpu_nj_create": (ctypes.c_int, [ctypes.c_int, ctypes.POINTER(_vp)]),
@@ -271,6 +302,31 @@ class Context:
         fn = self._lib.cwgpu_align_pairs_plain if plain else self._lib.cwgpu_align_pairs
         self._check(fn(self._h, _ptr(pr), n, _ptr(dist), _ptr(st)), "cwgpu_align_pairs")
         return (dist[:n], st[:n]) if stats else dist[:n]
+
+    def fast_align_pairs(self, pairs, fparams, stats=False):
+        """Quick k-tuple distances (FastPairwiseAlign) of pairs [P, 2]: float64."""
+        pr = np.ascontiguousarray(np.asarray(pairs, dtype=np.int32).reshape(-1, 2))
+        n = len(pr)
+        fp = fparams if isinstance(fparams, FastParams) else FastParams.from_dict(fparams)
+        dist = np.zeros(max(n, 1), dtype=np.float64)
+        st = np.zeros(max(n, 1), dtype=FAST_STATS_DTYPE) if stats else None
+        self._check(self._lib.cwgpu_fast_align_pairs(self._h, ctypes.byref(fp), _ptr(pr), n, _ptr(dist), _ptr(st)),
+                    "cwgpu_fast_align_pairs")
+        return (dist[:n], st[:n]) if stats else dist[:n]
+
+    def fast_align_pairs_device(self, fparams, d_pairs, d_order, npairs, d_dist, d_stats=None, stream=None):
+        fp = fparams if isinstance(fparams, FastParams) else FastParams.from_dict(fparams)
+        self._check(self._lib.cwgpu_fast_align_pairs_device(self._h, ctypes.byref(fp), d_pairs, d_order, int(npairs),
+                                                            d_dist, d_stats, stream), "cwgpu_fast_align_pairs_device")
+
+    def fast_pairwise_align(self, fparams, i_start, i_end, j_start, j_end, elements, dist_size, stats=False):
+        npairs = range_pair_count(self.nseqs, i_start, i_end, j_start, j_end)
+        fp = fparams if isinstance(fparams, FastParams) else FastParams.from_dict(fparams)
+        st = np.zeros(max(npairs, 1), dtype=FAST_STATS_DTYPE) if stats else None
+        rc = self._lib.cwgpu_fast_pairwise_align(self._h, ctypes.byref(fp), i_start, i_end, j_start, j_end,
+                                                 _ptr(elements), int(dist_size), _ptr(st))
+        self._check(rc, "cwgpu_fast_pairwise_align")
+        return st[:npairs] if stats else None
 
     def pairwise_align(self, i_start, i_end, j_start, j_end, elements, dist_size, stats=False):
         npairs = range_pair_count(self.nseqs, i_start, i_end, j_start, j_end)

@@ -196,3 +196,59 @@ class FullPairwiseAlign(PairwiseAlignBase):
                     mm = np.float32(100 * int(stats["n_ident"][q])) / np.float32(min(res[si], res[sj]))
                 print(f"Sequences ({si + 1}:{sj + 1}) Aligned. Score:  {int(mm)}")
                 q += 1
+
+
+class FastPairwiseAlign(PairwiseAlignBase):
+    """GB300 drop-in for clustalw::FastPairwiseAlign (quick k-tuple distances,
+    pairwise/FastPairwiseAlign.cpp:20-139). `fast_params` are the userParameters
+    values it reads (native.FastParams or a dict of its fields); by default the
+    reference's protein or DNA defaults for the sequences' type."""
+
+    def __init__(self, fast_params=None, dna=False, display_info=False, device=0, context=None):
+        self.fast_params = fast_params
+        self.dna = dna
+        self.display_info = display_info
+        self._ctx = context
+        self._device = device
+        self.last_stats = None
+
+    def _context(self):
+        if self._ctx is None:
+            self._ctx = native.Context(self._device)
+        return self._ctx
+
+    def pairwiseAlign(self, alignPtr, distMat, iStart, iEnd, jStart, jEnd):
+        numSeqs = alignPtr.getNumSeqs()
+        if distMat.getSize() != numSeqs + 1:
+            sys.stdout.write("The distance matrix is not the right size!\nNeed to terminate program.\n")
+            raise SystemExit(1)
+        if iStart < 0 or iEnd < iStart or jStart < 0 or jEnd < jStart:
+            sys.stdout.write("The range for pairwise Alignment is incorrect.\nNeed to terminate program.\n")
+            raise SystemExit(1)
+        fp = self.fast_params
+        if fp is None:
+            fp = native.FastParams.defaults(self.dna, alignPtr.getMaxAlnLength())
+        ctx = self._context()
+        ctx.upload_seqs(alignPtr.sequences())
+        stats = ctx.fast_pairwise_align(fp, iStart, iEnd, jStart, jEnd, distMat.getElements(), distMat.getSize(),
+                                        stats=True)
+        self.last_stats = stats
+        if self.display_info:
+            self._print_info(alignPtr, fp, stats, iStart, iEnd, jStart, jEnd)
+
+    def _print_info(self, aln, fp, stats, iStart, iEnd, jStart, jEnd):
+        """utilityObject->info lines of FastPairwiseAlign.cpp:107-118."""
+        fp = fp if isinstance(fp, native.FastParams) else native.FastParams.from_dict(fp)
+        n = aln.getNumSeqs()
+        q = 0
+        for si in range(max(0, iStart), min(n, iEnd)):
+            for sj in range(max(si + 1, jStart + 1), min(n, jEnd)):
+                score = int(stats["score"][q])
+                calc = float(score)
+                if score and fp.percent:
+                    calc = (calc / float(min(aln.getSeqLength(si + 1), aln.getSeqLength(sj + 1)))) * 100.0
+                if calc > 0.1:
+                    print(f"Sequences ({si + 1}:{sj + 1}) Aligned. Score: {calc:g}")
+                else:
+                    print(f"Sequences ({si + 1}:{sj + 1}) Not Aligned")
+                q += 1

@@ -23,6 +23,7 @@
 #include <vector>
 
 #include "cwgpu.h"
+#include "cwgpu_context.h"
 #include "cwgpu_device.cuh"
 
 namespace {
@@ -70,39 +71,7 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
 
 }  // namespace
 
-struct cwgpu_context {
-    int device = 0;
-    int sm_count = 0;
-    cudaStream_t stream = nullptr;
-    bool has_matrix = false, has_params = false, has_seqs = false;
-    int32_t matrix[CWGPU_NUMRES * CWGPU_NUMRES];
-    cwgpu_params params;
-    int nseqs = 0;
-    int lmax = 0;
-    std::vector<int32_t> lens;
-    std::vector<int64_t> offs;
-    std::vector<int8_t> host_codes;  // original codes, for nres and the remap
-    int K = 0;                       // codes present in the sequences
-    int dense_of[CWGPU_NUMRES];      // original code -> dense index, -1 if absent
-    int code_of[CWGPU_NUMRES];       // dense index -> original code
-    int tiny_m = 32, tiny_n = 16;    // Myers-Miller frames solved one per lane
-    int8_t* d_codes = nullptr;
-    int64_t* d_offs = nullptr;
-    int32_t* d_lens = nullptr;
-    int32_t* d_nres = nullptr;
-    int32_t* d_matrix = nullptr;
-    int32_t* d_go = nullptr;
-    int go_len = 0;
-    int2* d_scratch = nullptr;
-    size_t scratch_bytes = 0;
-    unsigned long long* d_counter = nullptr;  // [0] queue head, [1..3] cell counts
-    int* d_err = nullptr;
-    int grid = 0;
-    int grid_K = -1;  // K the grid size was computed for
-    bool derived_dirty = true;
-    unsigned generation = 0;  // bumped whenever device inputs or scratch move
-    std::string last_error;
-};
+// struct cwgpu_context: cwgpu_context.h (shared with the quick-distance path).
 
 struct cwgpu_plan {
     cwgpu_context* ctx = nullptr;
@@ -372,6 +341,7 @@ void cwgpu_destroy(cwgpu_context* ctx) {
     dfree(ctx->d_scratch);
     dfree(ctx->d_counter);
     dfree(ctx->d_err);
+    cwgpu_fast_release(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }

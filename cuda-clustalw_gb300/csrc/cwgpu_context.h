@@ -1,0 +1,53 @@
+// cwgpu_context.h - the context behind the opaque cwgpu_context handle of
+// cwgpu.h, shared by the translation units of the library (not installed).
+#ifndef CWGPU_CONTEXT_H
+#define CWGPU_CONTEXT_H
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "cwgpu.h"
+
+struct cwgpu_fast_state;
+// Frees the quick-distance tables of a context (cwgpu_fast.cu).
+void cwgpu_fast_release(cwgpu_context* ctx);
+
+struct cwgpu_context {
+    int device = 0;
+    int sm_count = 0;
+    cudaStream_t stream = nullptr;
+    bool has_matrix = false, has_params = false, has_seqs = false;
+    int32_t matrix[CWGPU_NUMRES * CWGPU_NUMRES];
+    cwgpu_params params;
+    int nseqs = 0;
+    int lmax = 0;
+    std::vector<int32_t> lens;
+    std::vector<int64_t> offs;
+    std::vector<int8_t> host_codes;  // original codes, for nres and the remap
+    int K = 0;                       // codes present in the sequences
+    int dense_of[CWGPU_NUMRES];      // original code -> dense index, -1 if absent
+    int code_of[CWGPU_NUMRES];       // dense index -> original code
+    int tiny_m = 32, tiny_n = 16;    // Myers-Miller frames solved one per lane
+    int8_t* d_codes = nullptr;
+    int64_t* d_offs = nullptr;
+    int32_t* d_lens = nullptr;
+    int32_t* d_nres = nullptr;
+    int32_t* d_matrix = nullptr;
+    int32_t* d_go = nullptr;
+    int go_len = 0;
+    int2* d_scratch = nullptr;
+    size_t scratch_bytes = 0;
+    unsigned long long* d_counter = nullptr;  // [0] queue head, [1..3] cell counts
+    int* d_err = nullptr;
+    int grid = 0;
+    int grid_K = -1;  // K the grid size was computed for
+    bool derived_dirty = true;
+    unsigned generation = 0;  // bumped whenever device inputs or scratch move
+    std::string last_error;
+    cwgpu_fast_state* fast = nullptr;  // quick-distance tables (cwgpu_fast.cu), built on first use
+};
+
+#endif  // CWGPU_CONTEXT_H

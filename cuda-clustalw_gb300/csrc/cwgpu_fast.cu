@@ -1,0 +1,734 @@
+// cwgpu_fast.cu - quick k-tuple distances (ClustalW's FastPairwiseAlign) on sm_103a.
+//
+// Computes what clustalw::FastPairwiseAlign::pairwiseAlign computes
+// (CPU/clustalw-2.0.11/src/pairwise/FastPairwiseAlign.cpp:20-400) for every
+// pair, bit-identically: the Wilbur-Lipman k-tuple diagonal method. Per pair:
+//   count    k-tuple hits per diagonal (vn1 - vn2 + l2)               :198-219
+//   select   the top `signif` diagonals after the reference's quicksort :221-241
+//   flag     diagonals within `window` of a selected one
+//   chain    for every k-tuple of seq 1 (ascending) and every match in
+//            seq 2 (descending position) on a flagged diagonal, the A-loop
+//            that extends or opens a fragment, fragments kept in a list
+//            sorted by score (putFrag)                                  :246-398
+//   score    the best fragment's score, as percent of the shorter length
+//
+// GB300 form: one warp per pair (a CTA of 32 threads), pairs taken longest
+// first from an atomic queue. The lanes count hits with shared-memory
+// atomics over per-sequence k-tuple position lists (built once per sequence
+// set by k_fast_prep), select the top diagonals in parallel, and enumerate
+// the flagged matches of each k-tuple in the reference's order; lane 0 alone
+// runs the fragment chaining, which is a sequential walk of a linked list, on
+// a shared-memory fragment table with 16-bit fields.
+//
+// Selection: the reference sorts the diagonal counts of positions
+// 1..tl1-1 ascending with its own quicksort and flags around the diagonals that
+// land in positions tl1-signif+1..tl1 (position tl1 itself is never sorted).
+// Only which diagonals land there matters. When the boundary value of the top
+// positions is not shared by more diagonals than fit, that set is every
+// diagonal above (or at) the boundary and no sort is needed; otherwise lane 0
+// replays the reference's quicksort, restricted to the sub-ranges that contain
+// top positions (the other sub-ranges cannot change them).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdint>
+#include <cstring>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include "cwgpu.h"
+#include "cwgpu_context.h"
+
+namespace cwfast {
+
+constexpr int kMaxLimit = 4096;  // k-tuple codes (25^2 protein, 4^6 DNA)
+constexpr int kMaxLen = 8191;    // longest sequence (16-bit fields, fs <= ktup * L < 2^15)
+
+struct Params {
+    int dna, ktup, window, window_gap, signif, percent, max_aa, max_aln;
+    int limit;  // number of k-tuple codes
+    int pot[8];
+};
+
+// DNA residue codes of the reference's mask (FastPairwiseAlign.cpp:163-164):
+// A C G T U -> 0 1 2 3 3, anything else invalid.
+__device__ __forceinline__ int aa2dna(int c) {
+    return c == 0 ? 0 : c == 2 ? 1 : c == 6 ? 2 : (c == 18 || c == 19) ? 3 : -1;
+}
+
+// Per sequence: kcode[p] = 1 + k-tuple code of the k-tuple starting at
+// 0-based position p (0 if it has an invalid residue or runs off the end),
+// and the 1-based positions of every code, grouped by code (CSR): positions of
+// code c are pos[start[c] .. start[c+1]) in sequence-local indices.
+__global__ void k_fast_prep(const int8_t* orig, const int64_t* offs, const int32_t* lens, Params P,
+                            int16_t* kcode, uint16_t* pos, int32_t* start) {
+    extern __shared__ int hist[];  // limit + 2
+    const int s = blockIdx.x;
+    const int L = lens[s];
+    const int64_t off = offs[s];
+    int32_t* st = start + (size_t)s * (P.limit + 2);
+    for (int c = threadIdx.x; c < P.limit + 2; c += blockDim.x) hist[c] = 0;
+    __syncthreads();
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+        int code = 0;
+        if (p + P.ktup <= L) {
+            code = 1;
+            for (int j = 0; j < P.ktup; ++j) {
+                int r = orig[off + p + j];
+                if (P.dna) r = aa2dna(r);
+                if (r < 0 || r > (P.dna ? 3 : P.max_aa)) {
+                    code = 0;
+                    break;
+                }
+                code += r * P.pot[j];
+            }
+        }
+        kcode[off + p] = (int16_t)code;
+        if (code) atomicAdd(&hist[code], 1);
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int c = 0; c <= P.limit; ++c) {
+            const int h = hist[c];
+            st[c] = acc;
+            hist[c] = acc;  // cursor
+            acc += h;
+        }
+        st[P.limit + 1] = acc;
+    }
+    __syncthreads();
+    for (int p = threadIdx.x; p < L; p += blockDim.x) {
+        const int code = kcode[off + p];
+        if (code) {
+            const int k = atomicAdd(&hist[code], 1);
+            pos[off + k] = (uint16_t)(p + 1);
+        }
+    }
+}
+
+struct Args {
+    const int16_t* kcode;
+    const uint16_t* pos;
+    const int32_t* start;
+    const int64_t* offs;
+    const int32_t* lens;
+    const int32_t* pairs;  // [npairs][2] 0-based (si, sj)
+    const int32_t* order;  // processing order (longest first)
+    long long npairs;
+    double* dist;
+    cwgpu_fast_stats* stats;
+    unsigned long long* counter;
+    Params P;
+    int lmax;  // longest sequence of the set (sizes the shared regions)
+};
+
+// Shared memory of one pair (one CTA), sizes from lmax:
+//   U       union: counts int32[T] + diag int32[T] (count/select), then the
+//           fragments: v1 | v2 << 16 (uint32[FR]), score int16[FR] and the
+//           score-sorted list R uint16[FR] (chain)
+//   flag    uint8[T], flagged uint16[NF], last uint16[NF], kc2 int16[lmax+1]
+// with T = 2*lmax + 2 diagonals, FR = 2*max_aln + 2 fragments and NF the most
+// diagonals that can be flagged, signif * (2*window + 1) (at most T); `last`
+// (the newest fragment on each flagged diagonal) is indexed like `flagged`.
+struct Smem {
+    int* cnt;
+    int* diag;
+    unsigned* vv;     // fragment v1 | v2 << 16
+    int16_t* fsa;     // fragment score
+    uint16_t* R;      // the score-sorted list, tail first
+    uint8_t* flag;
+    uint16_t* flagged;
+    uint16_t* last;
+    int16_t* kc2;
+};
+
+__host__ __device__ inline size_t max_flagged(int lmax, int signif, int window) {
+    const size_t T = 2 * (size_t)lmax + 2, nf = (size_t)signif * (2 * (size_t)window + 1);
+    return nf < T ? nf : T;
+}
+
+__host__ __device__ inline size_t smem_bytes(int lmax, int max_aln, size_t NF, size_t* offs_out = nullptr) {
+    const size_t T = 2 * (size_t)lmax + 2, FR = 2 * (size_t)max_aln + 2;
+    size_t u = 8 * T > 8 * FR ? 8 * T : 8 * FR;
+    u = (u + 15) & ~(size_t)15;
+    size_t off = u;
+    size_t o_flag = off;
+    off += (T + 15) & ~(size_t)15;
+    size_t o_flagged = off;
+    off += (2 * NF + 15) & ~(size_t)15;
+    size_t o_last = off;
+    off += (2 * NF + 15) & ~(size_t)15;
+    size_t o_kc2 = off;
+    off += (2 * ((size_t)lmax + 1) + 15) & ~(size_t)15;
+    if (offs_out) {
+        offs_out[0] = o_flag;
+        offs_out[1] = o_flagged;
+        offs_out[2] = o_last;
+        offs_out[3] = o_kc2;
+    }
+    return off;
+}
+
+__device__ Smem carve(int lmax, int max_aln, size_t NF) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    size_t o[4];
+    smem_bytes(lmax, max_aln, NF, o);
+    const size_t T = 2 * (size_t)lmax + 2, FR = 2 * (size_t)max_aln + 2;
+    Smem S;
+    S.cnt = reinterpret_cast<int*>(smem);
+    S.diag = S.cnt + T;
+    S.vv = reinterpret_cast<unsigned*>(smem);
+    S.fsa = reinterpret_cast<int16_t*>(smem + 4 * FR);
+    S.R = reinterpret_cast<uint16_t*>(smem + 6 * FR);
+    S.flag = smem + o[0];
+    S.flagged = reinterpret_cast<uint16_t*>(smem + o[1]);
+    S.last = reinterpret_cast<uint16_t*>(smem + o[2]);
+    S.kc2 = reinterpret_cast<int16_t*>(smem + o[3]);
+    return S;
+}
+
+constexpr unsigned kFull = 0xffffffffu;
+
+__device__ __forceinline__ int warp_max(int v) {
+    for (int o = 16; o; o >>= 1) v = max(v, __shfl_xor_sync(kFull, v, o));
+    return v;
+}
+__device__ __forceinline__ int warp_sum(int v) {
+    for (int o = 16; o; o >>= 1) v += __shfl_xor_sync(kFull, v, o);
+    return v;
+}
+
+// The reference's quicksort (desQuickSort, FastPairwiseAlign.cpp:585-658) of
+// a[1..size-1] ascending with b permuted alongside, run only on sub-ranges
+// that overlap [want_lo, size-1]: a partition permutes only inside its own
+// range, so the other sub-ranges cannot change positions want_lo and up.
+// Lane 0 only. The explicit stack holds at most log2(size) + 1 ranges, as the
+// reference's (it always continues with the smaller part).
+__device__ void top_quick_sort(int* a, int* b, int size, int want_lo) {
+    int lst[50], ust[50], p = 1;
+    lst[1] = 1;
+    ust[1] = size - 1;
+    while (p > 0) {
+        if (lst[p] >= ust[p] || ust[p] < want_lo) {
+            p--;
+            continue;
+        }
+        int i = lst[p] - 1, j = ust[p];
+        const int piv = a[j];
+        while (i < j) {
+            for (i = i + 1; a[i] < piv; i++)
+                ;
+            for (j = j - 1; j > i; j--)
+                if (a[j] <= piv) break;
+            if (i < j) {
+                int t = a[i]; a[i] = a[j]; a[j] = t;
+                t = b[i]; b[i] = b[j]; b[j] = t;
+            }
+        }
+        j = ust[p];
+        int t = a[i]; a[i] = a[j]; a[j] = t;
+        t = b[i]; b[i] = b[j]; b[j] = t;
+        if (i - lst[p] < ust[p] - i) {
+            lst[p + 1] = lst[p];
+            ust[p + 1] = i - 1;
+            lst[p] = i + 1;
+        } else {
+            lst[p + 1] = i + 1;
+            ust[p + 1] = ust[p];
+            ust[p] = i - 1;
+        }
+        p = p + 1;
+        if (p >= 49) {  // cannot happen (depth <= log2(size) + 1); keep the stack in bounds
+            p = 48;
+        }
+    }
+}
+
+__device__ __forceinline__ bool frag_rel_pos(int a1, int b1, int a2, int b2, int ktup) {
+    if (a1 - b1 == a2 - b2) return a2 < a1;
+    return a2 + ktup - 1 < a1 && b2 + ktup - 1 < b1;
+}
+
+// One pair on one warp.
+__device__ void fast_pair(const Args& A, const Smem& S, long long q) {
+    const Params& P = A.P;
+    const int lane = threadIdx.x & 31;
+    const int si = A.pairs[2 * q], sj = A.pairs[2 * q + 1];
+    const int l1 = A.lens[si], l2 = A.lens[sj];
+    const int64_t o1 = A.offs[si], o2 = A.offs[sj];
+    const int tl1 = l1 + l2 - 1;
+    const int ktup = P.ktup;
+    const int16_t* kc1 = A.kcode + o1;
+    const uint16_t* pos2 = A.pos + o2;
+    const int32_t* st2 = A.start + (size_t)sj * (P.limit + 2);
+
+    // ---- count hits per diagonal (:198-219)
+    for (int d = lane; d <= tl1 + 1; d += 32) S.cnt[d] = 0;
+    for (int p = lane; p < l2; p += 32) S.kc2[p + 1] = A.kcode[o2 + p];
+    __syncwarp();
+    for (int p1 = 1 + lane; p1 <= l1 - ktup + 1; p1 += 32) {
+        const int c = kc1[p1 - 1];
+        if (!c) continue;
+        const int b = __ldg(st2 + c), e = __ldg(st2 + c + 1);
+#pragma unroll 4
+        for (int k = b; k < e; ++k) atomicAdd(&S.cnt[p1 - __ldg(pos2 + k) + l2], 1);
+    }
+    __syncwarp();
+
+    // ---- select the top diagonals (:221-241)
+    const int jlo = max(1, tl1 - P.signif + 1);  // first top position
+    const int kk = tl1 - jlo;                    // sorted top positions jlo..tl1-1
+    int mode = 0;                                 // 0: none, 1: count > T, 2: count >= T, 3: sorted
+    int T = 0;
+    if (kk > 0) {
+        int cur = 0x7fffffff, got = 0, eq = 0;
+        for (;;) {  // k-th largest of cnt[1..tl1-1], with multiplicity
+            int v = -1;
+            for (int d = 1 + lane; d <= tl1 - 1; d += 32) {
+                const int x = S.cnt[d];
+                if (x < cur) v = max(v, x);
+            }
+            v = warp_max(v);
+            if (v < 0) break;  // fewer than kk values below cur (cannot happen: kk <= tl1 - 1)
+            int c = 0;
+            for (int d = 1 + lane; d <= tl1 - 1; d += 32) c += S.cnt[d] == v;
+            c = warp_sum(c);
+            got += c;
+            cur = v;
+            if (got >= kk) {
+                eq = c;
+                break;
+            }
+        }
+        T = cur;
+        const int gt = got - eq;
+        if (T <= 0) mode = 1;                // every positive count is in the top positions
+        else if (eq == kk - gt) mode = 2;    // all diagonals at the boundary fit
+        else mode = 3;                       // ties straddle the boundary: the reference's sort decides
+    }
+    for (int d = lane; d <= tl1 + 1; d += 32) S.flag[d] = 0;
+    __syncwarp();
+    if (mode == 3) {
+        for (int d = lane; d <= tl1; d += 32) S.diag[d] = d;
+        __syncwarp();
+        if (lane == 0) {
+            top_quick_sort(S.cnt, S.diag, tl1, jlo);
+            for (int i = tl1 - 1; i >= jlo; --i)
+                if (S.cnt[i] > 0) {
+                    const int c = S.diag[i];
+                    for (int l = max(1, c - P.window); l <= min(tl1, c + P.window); ++l) S.flag[l] = 1;
+                }
+        }
+    } else if (mode != 0) {
+        for (int d = 1 + lane; d <= tl1 - 1; d += 32) {
+            const int x = S.cnt[d];
+            if (x > 0 && (x > T || (mode == 2 && x == T)))
+                for (int l = max(1, d - P.window); l <= min(tl1, d + P.window); ++l) S.flag[l] = 1;
+        }
+    }
+    if (lane == 0 && tl1 >= 1 && S.cnt[tl1] > 0)  // position tl1 keeps its own diagonal
+        for (int l = max(1, tl1 - P.window); l <= tl1; ++l) S.flag[l] = 1;
+    __syncwarp();
+    // Flagged diagonals in ascending order. At most signif centres with
+    // 2*window+1 diagonals each can be flagged, which sizes the list (the
+    // bound check never fails).
+    const int nf_cap = (int)max_flagged(A.lmax, P.signif, P.window);
+    int nf = 0;
+    for (int base = 1; base <= tl1; base += 32) {
+        const int d = base + lane;
+        const bool f = d <= tl1 && S.flag[d];
+        const unsigned m = __ballot_sync(kFull, f);
+        const int at = nf + __popc(m & ((1u << lane) - 1));
+        if (f && at < nf_cap) S.flagged[at] = (uint16_t)d;
+        nf += __popc(m);
+    }
+    nf = min(nf, nf_cap);
+    for (int f = lane; f < nf; f += 32) S.last[f] = 0;
+    __syncwarp();
+
+    // ---- chain fragments (:246-398), the whole warp together.
+    // The reference keeps every fragment in a list sorted by score (putFrag)
+    // and, for each match on a flagged diagonal, walks the list from the best
+    // fragment to the first one the match can follow (the A-loop). Here the
+    // list is the array R[0 .. nfr) of fragment numbers in list order
+    // reversed, R[nfr-1] being the head (maxSoFar): a walk from the head is a
+    // 32-wide scan down from the top of R, and an insertion, which putFrag
+    // makes close to the head, shifts only the entries above it.
+    int nfr = 0, currFrag = 0;
+    bool partial = false;
+    for (int i = 1; i <= l1 - ktup + 1 && !partial; ++i) {
+        const int c1 = kc1[i - 1];
+        if (!c1) continue;
+        for (int base = 0; base < nf && !partial; base += 32) {
+            const int k = base + lane;
+            int vn2 = 0;
+            bool hit = false;
+            if (k < nf) {
+                vn2 = i - (int)S.flagged[k] + l2;  // osptr = i - vn2 + l2 = flagged[k]
+                hit = vn2 >= 1 && vn2 <= l2 - ktup + 1 && S.kc2[vn2] == c1;
+            }
+            unsigned m = __ballot_sync(kFull, hit);
+            // ascending diagonal = descending vn2: the order of the reference's list
+            while (m && !partial) {
+                const int t = __ffs(m) - 1;
+                m &= m - 1;
+                const int fi = base + t;  // position of the diagonal in `flagged`
+                const int osptr = S.flagged[fi];
+                const int v2 = i - osptr + l2;
+                // the A-loop: first fragment from the head this match can follow
+                int found = 0;
+                for (int kb = 0; kb < nfr; kb += 32) {
+                    const int kk2 = kb + lane;
+                    int idx = 0;
+                    bool ok = false;
+                    if (kk2 < nfr) {
+                        idx = S.R[nfr - 1 - kk2];
+                        const unsigned vv = S.vv[idx];
+                        ok = frag_rel_pos(i, v2, (int)(vv & 0xffffu), (int)(vv >> 16), ktup);
+                    }
+                    const unsigned mm = __ballot_sync(kFull, ok);
+                    if (mm) {
+                        found = __shfl_sync(kFull, idx, __ffs(mm) - 1);
+                        break;
+                    }
+                }
+                int fs = ktup;
+                if (found) {
+                    const unsigned vv = S.vv[found];
+                    const int tv1 = (int)(vv & 0xffffu), tv2 = (int)(vv >> 16);
+                    const int tfs = S.fsa[found];
+                    if (i - v2 == tv1 - tv2) {
+                        fs = tfs + (i > tv1 + (ktup - 1) ? ktup : i - tv1);
+                    } else {
+                        const int lf = S.last[fi];
+                        int subt1 = ktup;
+                        if (lf) {
+                            const int lv1 = (int)(S.vv[lf] & 0xffffu);
+                            subt1 = S.fsa[lf] + (i > lv1 + (ktup - 1) ? ktup : i - lv1);
+                        }
+                        const int subt2 = tfs - P.window_gap + ktup;
+                        fs = subt2 > subt1 ? subt2 : subt1;
+                    }
+                }
+                currFrag = nfr + 1;
+                if (currFrag >= 2 * P.max_aln) {
+                    partial = true;
+                    break;
+                }
+                // putFrag: before the first fragment from the head whose score
+                // is not above fs (the tail if none)
+                int kins = nfr;
+                for (int kb = 0; kb < nfr; kb += 32) {
+                    const int kk2 = kb + lane;
+                    const bool le = kk2 < nfr && S.fsa[S.R[nfr - 1 - kk2]] <= fs;
+                    const unsigned mm = __ballot_sync(kFull, le);
+                    if (mm) {
+                        kins = kb + __ffs(mm) - 1;
+                        break;
+                    }
+                }
+                const int pnew = nfr - kins;  // the new fragment's index in R
+                for (int top = nfr - 1; top >= pnew; top -= 32) {  // R[pnew..nfr) up one, top chunk first
+                    const int x = top - lane;
+                    uint16_t v = 0;
+                    if (x >= pnew) v = S.R[x];
+                    __syncwarp();
+                    if (x >= pnew) S.R[x + 1] = v;
+                    __syncwarp();
+                }
+                if (lane == 0) {
+                    S.vv[currFrag] = (unsigned)i | ((unsigned)v2 << 16);
+                    S.fsa[currFrag] = (int16_t)fs;
+                    S.R[pnew] = (uint16_t)currFrag;
+                    S.last[fi] = (uint16_t)currFrag;
+                }
+                __syncwarp();
+                nfr = currFrag;
+            }
+        }
+    }
+
+    // ---- distance (:88-103), in double as the reference
+    if (lane == 0) {
+        const int score = nfr ? S.fsa[S.R[nfr - 1]] : 0;
+        double calc = 0.0;
+        if (nfr) {
+            calc = (double)score;
+            if (P.percent) calc = __dmul_rn(__ddiv_rn(calc, (double)min(l1, l2)), 100.0);
+        }
+        A.dist[q] = __ddiv_rn(__dsub_rn(100.0, calc), 100.0);
+        if (A.stats) {
+            cwgpu_fast_stats st;
+            st.score = score;
+            st.frags = currFrag;
+            st.partial = partial ? 1 : 0;
+            st.pad = 0;
+            A.stats[q] = st;
+        }
+    }
+    __syncwarp();
+}
+
+__global__ void __launch_bounds__(32) k_fast(Args A) {
+    const Smem S = carve(A.lmax, A.P.max_aln, max_flagged(A.lmax, A.P.signif, A.P.window));
+    const int lane = threadIdx.x;
+    for (;;) {
+        unsigned long long k = 0;
+        if (lane == 0) k = atomicAdd(A.counter, 1ULL);
+        k = __shfl_sync(kFull, k, 0);
+        if (k >= (unsigned long long)A.npairs) break;
+        fast_pair(A, S, A.order ? A.order[k] : (long long)k);
+    }
+}
+
+}  // namespace cwfast
+
+using namespace cwfast;
+
+// Per-context tables of the quick path, rebuilt when the sequences or the
+// k-tuple parameters change.
+struct cwgpu_fast_state {
+    unsigned generation = ~0u;
+    int key_dna = -1, key_ktup = -1, key_max_aa = -1;
+    int8_t* d_orig = nullptr;
+    int16_t* d_kcode = nullptr;
+    uint16_t* d_pos = nullptr;
+    int32_t* d_start = nullptr;
+    int limit = 0;
+    unsigned long long* d_counter = nullptr;
+    size_t smem_set = 0;
+};
+
+void cwgpu_fast_release(cwgpu_context* ctx) {
+    if (!ctx || !ctx->fast) return;
+    cwgpu_fast_state* F = ctx->fast;
+    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete F;
+    ctx->fast = nullptr;
+}
+
+namespace {
+
+int ffail(cwgpu_context* ctx, int code, const std::string& msg) {
+    ctx->last_error = msg;
+    return code;
+}
+
+#define FAST_CUDA(ctx, call)                                                                               \
+    do {                                                                                                   \
+        cudaError_t e_ = (call);                                                                           \
+        if (e_ != cudaSuccess)                                                                             \
+            return ffail(ctx, e_ == cudaErrorMemoryAllocation ? CWGPU_ERR_OOM : CWGPU_ERR_CUDA,          \
+                         std::string(#call) + ": " + cudaGetErrorString(e_));                              \
+    } while (0)
+
+int make_params(cwgpu_context* ctx, const cwgpu_fast_params* p, Params* P) {
+    if (!p) return CWGPU_ERR_ARG;
+    const int base = p->dna ? 4 : p->max_aa + 1;
+    if (p->ktup < 1 || p->ktup > 6 || base < 1 || p->max_aa < 0 || p->max_aa > 31 || p->window < 0 ||
+        p->window_gap < 0 || p->signif < 1)
+        return ffail(ctx, CWGPU_ERR_ARG, "k-tuple parameters out of range");
+    long long limit = 1;
+    for (int i = 0; i < p->ktup; ++i) limit *= base;
+    if (limit > kMaxLimit) return ffail(ctx, CWGPU_ERR_ARG, "too many k-tuple codes (ktup too large)");
+    memset(P, 0, sizeof(*P));
+    P->dna = p->dna ? 1 : 0;
+    P->ktup = p->ktup;
+    P->window = p->window;
+    P->window_gap = p->window_gap;
+    P->signif = p->signif;
+    P->percent = p->percent ? 1 : 0;
+    P->max_aa = p->max_aa;
+    P->max_aln = p->max_aln_length > 0 ? p->max_aln_length : 2 * ctx->lmax;
+    P->limit = (int)limit;
+    int v = 1;
+    for (int i = 0; i < p->ktup; ++i) {
+        P->pot[i] = v;
+        v *= base;
+    }
+    if (ctx->lmax > kMaxLen || (long long)P->ktup * ctx->lmax > 32767 || 2LL * P->max_aln + 2 > 65535)
+        return ffail(ctx, CWGPU_ERR_ARG, "sequences too long for the quick k-tuple path (8191 residues)");
+    return CWGPU_OK;
+}
+
+int ensure_tables(cwgpu_context* ctx, const Params& P) {
+    if (!ctx->fast) ctx->fast = new cwgpu_fast_state();
+    cwgpu_fast_state* F = ctx->fast;
+    if (F->generation == ctx->generation && F->key_dna == P.dna && F->key_ktup == P.ktup &&
+        F->key_max_aa == P.max_aa)
+        return CWGPU_OK;
+    FAST_CUDA(ctx, cudaSetDevice(ctx->device));
+    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    F->d_orig = nullptr;
+    F->d_kcode = nullptr;
+    F->d_pos = nullptr;
+    F->d_start = nullptr;
+    const size_t total = std::max<size_t>(ctx->host_codes.size(), 16);
+    const int ns = std::max(1, ctx->nseqs);
+    FAST_CUDA(ctx, cudaMalloc(&F->d_orig, total));
+    FAST_CUDA(ctx, cudaMalloc(&F->d_kcode, total * sizeof(int16_t)));
+    FAST_CUDA(ctx, cudaMalloc(&F->d_pos, total * sizeof(uint16_t)));
+    FAST_CUDA(ctx, cudaMalloc(&F->d_start, (size_t)ns * (P.limit + 2) * sizeof(int32_t)));
+    if (!F->d_counter) FAST_CUDA(ctx, cudaMalloc(&F->d_counter, sizeof(unsigned long long)));
+    FAST_CUDA(ctx, cudaMemcpy(F->d_orig, ctx->host_codes.data(), ctx->host_codes.size(), cudaMemcpyHostToDevice));
+    if (ctx->nseqs > 0) {
+        k_fast_prep<<<ctx->nseqs, 256, sizeof(int) * (P.limit + 2), ctx->stream>>>(
+            F->d_orig, ctx->d_offs, ctx->d_lens, P, F->d_kcode, F->d_pos, F->d_start);
+        FAST_CUDA(ctx, cudaGetLastError());
+        FAST_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    F->generation = ctx->generation;
+    F->key_dna = P.dna;
+    F->key_ktup = P.ktup;
+    F->key_max_aa = P.max_aa;
+    F->limit = P.limit;
+    return CWGPU_OK;
+}
+
+// Runs the pairs (device pointers) in `d_order` order on `st`; synchronous.
+int run_fast(cwgpu_context* ctx, const Params& P, const int32_t* d_pairs, const int32_t* d_order, long long npairs,
+             double* d_dist, cwgpu_fast_stats* d_stats, cudaStream_t st) {
+    cwgpu_fast_state* F = ctx->fast;
+    const size_t sm = smem_bytes(ctx->lmax, P.max_aln, max_flagged(ctx->lmax, P.signif, P.window));
+    if (sm > 227 * 1024) return ffail(ctx, CWGPU_ERR_ARG, "sequences too long for the quick path's shared memory");
+    if (sm > F->smem_set) {
+        FAST_CUDA(ctx, cudaFuncSetAttribute(k_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
+        F->smem_set = sm;
+    }
+    int per_sm = 0;
+    FAST_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast, 32, sm));
+    if (per_sm < 1) return ffail(ctx, CWGPU_ERR_ARG, "quick path does not fit one SM");
+    const long long grid = std::min<long long>((long long)per_sm * ctx->sm_count, std::max<long long>(npairs, 1));
+    Args A;
+    A.kcode = F->d_kcode;
+    A.pos = F->d_pos;
+    A.start = F->d_start;
+    A.offs = ctx->d_offs;
+    A.lens = ctx->d_lens;
+    A.pairs = d_pairs;
+    A.order = d_order;
+    A.npairs = npairs;
+    A.dist = d_dist;
+    A.stats = d_stats;
+    A.counter = F->d_counter;
+    A.P = P;
+    A.lmax = ctx->lmax;
+    FAST_CUDA(ctx, cudaMemsetAsync(F->d_counter, 0, sizeof(unsigned long long), st));
+    if (npairs > 0) {
+        k_fast<<<(unsigned)grid, 32, sm, st>>>(A);
+        FAST_CUDA(ctx, cudaGetLastError());
+    }
+    return CWGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int cwgpu_fast_align_pairs(cwgpu_context* ctx, const cwgpu_fast_params* p, const int32_t* pairs, int64_t npairs,
+                           double* dist_out, cwgpu_fast_stats* stats_out) {
+    if (!ctx || npairs < 0 || (npairs > 0 && (!pairs || !dist_out))) return CWGPU_ERR_ARG;
+    if (!ctx->has_seqs) return ffail(ctx, CWGPU_ERR_STATE, "sequences not set");
+    Params P;
+    int rc = make_params(ctx, p, &P);
+    if (rc) return rc;
+    for (int64_t q = 0; q < npairs; ++q) {
+        const int32_t a = pairs[2 * q], b = pairs[2 * q + 1];
+        if (a < 0 || b < 0 || a >= ctx->nseqs || b >= ctx->nseqs)
+            return ffail(ctx, CWGPU_ERR_ARG, "pair index outside the sequence set");
+    }
+    if (npairs == 0) return CWGPU_OK;
+    rc = ensure_tables(ctx, P);
+    if (rc) return rc;
+    // Longest pairs first: the hit count and the chain grow with l1 * l2.
+    std::vector<int32_t> order(npairs);
+    std::iota(order.begin(), order.end(), 0);
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        const long long wx = (long long)ctx->lens[pairs[2 * x]] * ctx->lens[pairs[2 * x + 1]];
+        const long long wy = (long long)ctx->lens[pairs[2 * y]] * ctx->lens[pairs[2 * y + 1]];
+        return wx > wy;
+    });
+    int32_t *d_pairs = nullptr, *d_order = nullptr;
+    double* d_dist = nullptr;
+    cwgpu_fast_stats* d_stats = nullptr;
+    cudaStream_t st = ctx->stream;
+    auto cleanup = [&]() {
+        if (d_pairs) cudaFree(d_pairs);
+        if (d_order) cudaFree(d_order);
+        if (d_dist) cudaFree(d_dist);
+        if (d_stats) cudaFree(d_stats);
+    };
+    cudaError_t e = cudaMalloc(&d_pairs, sizeof(int32_t) * 2 * npairs);
+    if (e == cudaSuccess) e = cudaMalloc(&d_order, sizeof(int32_t) * npairs);
+    if (e == cudaSuccess) e = cudaMalloc(&d_dist, sizeof(double) * npairs);
+    if (e == cudaSuccess && stats_out) e = cudaMalloc(&d_stats, sizeof(cwgpu_fast_stats) * npairs);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, st);
+    if (e != cudaSuccess) {
+        cleanup();
+        return ffail(ctx, e == cudaErrorMemoryAllocation ? CWGPU_ERR_OOM : CWGPU_ERR_CUDA,
+                     std::string("quick path set-up: ") + cudaGetErrorString(e));
+    }
+    rc = run_fast(ctx, P, d_pairs, d_order, npairs, d_dist, d_stats, st);
+    if (rc == CWGPU_OK) {
+        e = cudaMemcpyAsync(dist_out, d_dist, sizeof(double) * npairs, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess && stats_out)
+            e = cudaMemcpyAsync(stats_out, d_stats, sizeof(cwgpu_fast_stats) * npairs, cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        if (e != cudaSuccess) rc = ffail(ctx, CWGPU_ERR_CUDA, std::string("quick path: ") + cudaGetErrorString(e));
+    }
+    cleanup();
+    return rc;
+}
+
+int cwgpu_fast_align_pairs_device(cwgpu_context* ctx, const cwgpu_fast_params* p, const int32_t* d_pairs,
+                                  const int32_t* d_order, int64_t npairs, double* d_dist,
+                                  cwgpu_fast_stats* d_stats, void* stream) {
+    if (!ctx || npairs < 0 || (npairs > 0 && (!d_pairs || !d_dist))) return CWGPU_ERR_ARG;
+    if (!ctx->has_seqs) return ffail(ctx, CWGPU_ERR_STATE, "sequences not set");
+    Params P;
+    int rc = make_params(ctx, p, &P);
+    if (rc) return rc;
+    rc = ensure_tables(ctx, P);
+    if (rc) return rc;
+    return run_fast(ctx, P, d_pairs, d_order, npairs, d_dist, d_stats, stream ? (cudaStream_t)stream : ctx->stream);
+}
+
+int cwgpu_fast_pairwise_align(cwgpu_context* ctx, const cwgpu_fast_params* p, int32_t i_start, int32_t i_end,
+                              int32_t j_start, int32_t j_end, double* elements, int32_t dist_size,
+                              cwgpu_fast_stats* stats_out) {
+    if (!ctx || !elements) return CWGPU_ERR_ARG;
+    if (!ctx->has_seqs) return ffail(ctx, CWGPU_ERR_STATE, "sequences not set");
+    const int n = ctx->nseqs;
+    if (dist_size != n + 1) return ffail(ctx, CWGPU_ERR_ARG, "The distance matrix is not the right size!");
+    if (i_start < 0 || i_end < i_start || j_start < 0 || j_end < j_start)
+        return ffail(ctx, CWGPU_ERR_RANGE, "The range for pairwise Alignment is incorrect.");
+    // FastPairwiseAlign.cpp:65-84: i = iStart+1..iEnd, j = max(jStart+2, i+1)..jEnd
+    // (1-based), i.e. si in [iStart, iEnd), sj in [max(jStart+1, si+1), jEnd),
+    // held inside the sequence set.
+    std::vector<int32_t> pairs;
+    for (int si = i_start; si < std::min(n, i_end); ++si)
+        for (int sj = std::max(j_start + 1, si + 1); sj < std::min(n, j_end); ++sj) {
+            pairs.push_back(si);
+            pairs.push_back(sj);
+        }
+    const int64_t np = (int64_t)pairs.size() / 2;
+    std::vector<double> dist(std::max<int64_t>(np, 1));
+    int rc = cwgpu_fast_align_pairs(ctx, p, pairs.data(), np, dist.data(), stats_out);
+    if (rc) return rc;
+    for (int64_t q = 0; q < np; ++q) {
+        const int64_t a = pairs[2 * q + 1], b = pairs[2 * q];  // getIndex(si+1, sj+1), si < sj
+        elements[((a * (a + 1)) >> 1) + b] = dist[q];
+    }
+    return CWGPU_OK;
+}
+
+}  // extern "C"

@@ -243,6 +243,44 @@ int cwgpu_server_result(cwgpu_server* server, int64_t job_id, float* dist_out, c
 int cwgpu_server_release(cwgpu_server* server, int64_t job_id);
 int cwgpu_server_query(cwgpu_server* server, cwgpu_server_stats* out);
 
+/* ---- quick k-tuple distances --------------------------------------------- */
+
+/* The userParameters values FastPairwiseAlign::pairAlign reads
+ * (FastPairwiseAlign.cpp:176-183), after setProtParams/setDNAParams. Reference
+ * defaults (UserParameters.cpp:86-94, 133): protein ktup 1, window 5,
+ * window_gap 3, signif 5; DNA ktup 2, window 4, window_gap 5, signif 4;
+ * percent 1; max_aa 24. max_aln_length is Alignment::getMaxAlnLength() (0:
+ * twice the longest sequence of the context, what the reference computes). */
+typedef struct cwgpu_fast_params {
+    int32_t dna, ktup, window, window_gap, signif, percent, max_aa;
+    int32_t max_aln_length;
+} cwgpu_fast_params;
+
+/* Per pair: the best fragment's score, fragments made, and whether the
+ * reference's "(Partial alignment)" cut-off was hit (FastPairwiseAlign.cpp:273-278). */
+typedef struct cwgpu_fast_stats {
+    int32_t score, frags, partial, pad;
+} cwgpu_fast_stats;
+
+/* The drop-in for FastPairwiseAlign::pairwiseAlign(alignPtr, distMat, iStart,
+ * iEnd, jStart, jEnd) (CPU/clustalw-2.0.11/src/pairwise/FastPairwiseAlign.cpp:20-139)
+ * over the sequences of cwgpu_upload_seqs: every pair of its loops
+ * (i = iStart+1..iEnd, j = max(jStart+2, i+1)..jEnd, 1-based, held inside the
+ * set) gets (100 - calcScore) / 100 in double at getIndex(i, j). The same size
+ * and range checks as cwgpu_pairwise_align. Sequences up to 8191 residues. */
+int cwgpu_fast_pairwise_align(cwgpu_context* ctx, const cwgpu_fast_params* params, int32_t i_start,
+                              int32_t i_end, int32_t j_start, int32_t j_end, double* elements, int32_t dist_size,
+                              cwgpu_fast_stats* stats_out);
+/* Pair-list form: dist_out[q] for pairs[q] = (si, sj), 0-based. */
+int cwgpu_fast_align_pairs(cwgpu_context* ctx, const cwgpu_fast_params* params, const int32_t* pairs,
+                           int64_t npairs, double* dist_out, cwgpu_fast_stats* stats_out);
+/* Device-resident form: device pair list, optional device processing order
+ * (indices into the pair list, e.g. longest first; NULL: list order), device
+ * outputs; asynchronous on `stream` (a cudaStream_t; NULL: the context's). */
+int cwgpu_fast_align_pairs_device(cwgpu_context* ctx, const cwgpu_fast_params* params, const int32_t* d_pairs,
+                                  const int32_t* d_order, int64_t npairs, double* d_dist,
+                                  cwgpu_fast_stats* d_stats, void* stream);
+
 /* Waits for all work of the context and reports a kernel-side error flag. */
 int cwgpu_synchronize(cwgpu_context* ctx);
 
