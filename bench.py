@@ -21,6 +21,8 @@ divided by the time of the step.
   serve      served stream of independent jobs (continuous batching), p50/p99
   guide_tree NJTree::generateTree on the step's own distance matrix: GPU
              kernel (device-resident and through the C ABI) beside the oracle
+  quick      FastPairwiseAlign (k-tuple distances) on the same sequences:
+             GPU kernel beside the oracle on all host threads
 --impl reference times the reference CPU algorithm (the oracle port; the
 reference's own build is not available on the GPU host) on all host threads.
 """
@@ -70,6 +72,7 @@ def parse_args():
     ap.add_argument("--serve-rate", type=float, default=6.0, help="served job arrival rate (jobs/s)")
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-tree", action="store_true", help="skip the guide-tree leg")
+    ap.add_argument("--no-quick", action="store_true", help="skip the quick k-tuple distance leg")
     ap.add_argument("--autotune", action="store_true", help="pick the tiny-frame thresholds for this workload first")
     return ap.parse_args()
 
@@ -405,6 +408,79 @@ def guide_tree_leg(args, n, pairs, dist, device, peaks):
     }
 
 
+def quick_leg(args, ctx, seqs, pairs, device):
+    """Quick k-tuple distances (FastPairwiseAlign::pairwiseAlign,
+    pairwise/FastPairwiseAlign.cpp:20-400) over every pair of the workload with
+    the reference's default parameters: device-resident (CUDA events on the
+    launching stream), through the C ABI with host buffers, a seeded parity
+    sample against the oracle, and the oracle on all host threads."""
+    import torch
+
+    from clustalw_gb300 import native
+    from oracle import oracle
+
+    n = len(seqs)
+    fp = native.FastParams.defaults(0, 2 * max(len(x) for x in seqs))
+    lens = np.array([len(x) for x in seqs], dtype=np.int64)
+    order = np.argsort(-(lens[pairs[:, 0]] * lens[pairs[:, 1]]), kind="stable").astype(np.int32)
+    dev = torch.device("cuda", device)
+    d_pairs = torch.from_numpy(np.ascontiguousarray(pairs, dtype=np.int32)).to(dev)
+    d_order = torch.from_numpy(order).to(dev)
+    d_dist = torch.empty(len(pairs), dtype=torch.float64, device=dev)
+    stream = torch.cuda.Stream(device=dev)
+    torch.cuda.synchronize()
+    steps, warmup = max(1, args.steps), max(3, args.warmup)
+    times = []
+    for k in range(warmup + steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        ctx.fast_align_pairs_device(fp, d_pairs.data_ptr(), d_order.data_ptr(), len(pairs), d_dist.data_ptr(), None,
+                                    stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        if k >= warmup:
+            times.append(e0.elapsed_time(e1) / 1e3)
+    dev_s = statistics.median(times)
+    dist_dev = d_dist.cpu().numpy()
+    e2e = []
+    for k in range(min(steps, 3) + 1):
+        t = time.perf_counter()
+        ctx.upload_seqs(seqs)
+        d = ctx.fast_align_pairs(pairs, fp)
+        if k:
+            e2e.append(time.perf_counter() - t)
+    e2e_s = statistics.median(e2e)
+    # Parity sample and CPU baseline: the oracle on all host threads.
+    rng = np.random.default_rng(11)
+    samp = np.sort(rng.choice(len(pairs), size=min(len(pairs), 4000), replace=False))
+    threads = os.cpu_count() or 1
+    fpd = {k: int(getattr(fp, k)) for k, _ in native.FastParams._fields_}
+    t = time.perf_counter()
+    want = oracle.fast_pairs(seqs, fpd, pairs[samp], nthreads=threads)
+    cpu_s = time.perf_counter() - t
+    same = bool(np.array_equal(want["dist"].view(np.int64), dist_dev[samp].view(np.int64))
+                and np.array_equal(d.view(np.int64), dist_dev.view(np.int64)))
+    cpu_rate = len(samp) / cpu_s
+    return {
+        "metric": "pairs per second",
+        "value": len(pairs) / dev_s,
+        "unit": "pairs/s",
+        "ms_per_step": 1e3 * dev_s,
+        "pairs": int(len(pairs)),
+        "params": fpd,
+        "e2e": {"value": len(pairs) / e2e_s, "unit": "pairs/s", "ms_per_step": 1e3 * e2e_s,
+                "h2d_bytes_per_step": int(sum(len(x) for x in seqs) + 8 * len(pairs) + 12 * n),
+                "d2h_bytes_per_step": int(8 * len(pairs)),
+                "call": "cwgpu_upload_seqs + cwgpu_fast_align_pairs (host pair list in, host distances out)"},
+        "cpu_baseline": {"value": cpu_rate, "unit": "pairs/s", "cores": threads, "kind": "port",
+                         "sample": f"{len(samp)} of {len(pairs)} pairs (seeded uniform), {cpu_s:.1f} s on {threads} threads"},
+        "speedup_vs_cpu": (len(pairs) / dev_s) / cpu_rate,
+        "bit_exact_vs_oracle_sample": same,
+        "roofline": {"bound": "latency (per-pair sequential fragment chaining, one warp per pair)", "kernel": "k_fast"},
+        "gpu_launches": steps,
+    }
+
+
 # ---------------------------------------------------------------- GPU arm
 
 
@@ -607,6 +683,8 @@ def ours_arm(args):
                 line["serve"] = served_leg(args, matrix, params, local)
             if not args.no_tree:
                 line["guide_tree"] = guide_tree_leg(args, len(seqs), pairs, dist_out, local, peaks)
+            if not args.no_quick:
+                line["quick"] = quick_leg(args, ctx, seqs, pairs, local)
         print(json.dumps(line), flush=True)
     plan.close()
     ctx.close()

@@ -1,6 +1,7 @@
 // Link check for the C++ drop-ins: defines the reference's five process
 // globals (as CPU/clustalw-2.0.11/src/main.cpp:23-30 does), constructs
-// GpuFullPairwiseAlign behind a PairwiseAlignBase pointer and GpuNJTree behind
+// GpuFullPairwiseAlign and GpuFastPairwiseAlign behind a PairwiseAlignBase
+// pointer and GpuNJTree behind
 // a ClusterTreeAlgorithm pointer, and exits without calling them (this binary
 // is built and linked on a host without a GPU).
 #include "pairwise/PairwiseAlignBase.h"
@@ -11,6 +12,7 @@
 #include "substitutionMatrix/SubMatrix.h"
 #include "GpuFullPairwiseAlign.h"
 #include "GpuNJTree.h"
+#include "GpuFastPairwiseAlign.h"
 
 namespace clustalw {
 UserParameters* userParameters;
@@ -22,6 +24,8 @@ Stats* statsObject;
 
 int main() {
     clustalw::PairwiseAlignBase* p = new clustalw::GpuFullPairwiseAlign(0);
+    delete p;
+    p = new clustalw::GpuFastPairwiseAlign(0);
     delete p;
     // Deleted through the base pointer, as UnRootedClusterTree.cpp:248 does;
     // the drop-ins own no per-object device resources.

@@ -1,5 +1,5 @@
-"""The C++ drop-ins (cuda-clustalw_gb300/host/GpuFullPairwiseAlign.cpp and
-GpuNJTree.cpp) compile against the reference's own headers as C++98 and link
+"""The C++ drop-ins (cuda-clustalw_gb300/host/GpuFullPairwiseAlign.cpp,
+GpuFastPairwiseAlign.cpp and GpuNJTree.cpp) compile against the reference's own headers as C++98 and link
 against the reference's objects plus lib/libcwgpu.so. Runs only where the reference tree and its
 objects (oracle/build_ref.sh) are present."""
 import glob
@@ -26,6 +26,7 @@ def test_dropin_compiles_and_links(tmp_path, oracle_mod):
     cmd = ["g++", "-std=gnu++98", "-w", "-DOS_UNIX=1", *inc,
            os.path.join(REPO, "cuda-clustalw_gb300", "host", "GpuFullPairwiseAlign.cpp"),
            os.path.join(REPO, "cuda-clustalw_gb300", "host", "GpuNJTree.cpp"),
+           os.path.join(REPO, "cuda-clustalw_gb300", "host", "GpuFastPairwiseAlign.cpp"),
            os.path.join(REPO, "tests", "dropin_link_main.cpp"), *objs,
            "-L" + os.path.dirname(lib), "-lcwgpu", "-Wl,-rpath," + os.path.dirname(lib), "-o", out]
     subprocess.run(cmd, check=True)
