@@ -32,26 +32,27 @@ def partition_pairs(lens, pairs, nparts):
 
 
 def sharded_pairwise(seqs, pairs, align_fn, group=None):
-    """Run this rank's shard with `align_fn(seqs, pair_subset) -> float32 dists`
-    and gather every shard's distances on rank 0 of `group` (a
+    """Run this rank's shard with `align_fn(seqs, pair_subset) -> distances`
+    (float32 for the full stage, float64 for the quick k-tuple distances; the
+    dtype is kept) and gather every shard's distances on rank 0 of `group` (a
     torch.distributed process group, or None for one process). Returns the
     full distance array on rank 0 and None elsewhere."""
     pairs = np.asarray(pairs, dtype=np.int32).reshape(-1, 2)
     lens = [len(s) for s in seqs]
     if group is None:
-        return np.asarray(align_fn(seqs, pairs), dtype=np.float32)
+        return np.asarray(align_fn(seqs, pairs))
     import torch.distributed as dist
 
     world = dist.get_world_size(group)
     rank = dist.get_rank(group)
     shards = partition_pairs(lens, pairs, world)
     mine = shards[rank]
-    d = np.asarray(align_fn(seqs, pairs[mine]), dtype=np.float32)
+    d = np.asarray(align_fn(seqs, pairs[mine]))
     gathered = [None] * world if rank == 0 else None
     dist.gather_object((mine, d), gathered, dst=0, group=group)
     if rank != 0:
         return None
-    out = np.zeros(len(pairs), dtype=np.float32)
+    out = np.zeros(len(pairs), dtype=np.result_type(*[vals.dtype for _, vals in gathered]))
     for idx, vals in gathered:
         out[idx] = vals
     return out

@@ -63,3 +63,48 @@ def test_two_gloo_ranks_assemble_the_full_result(tmp_path):
     seqs = [np.zeros(int(L), np.int8) for L in rng.integers(5, 400, size=37)]
     want = fake_align(seqs, all_pairs(37))
     assert np.array_equal(np.load(out), want)
+
+
+def quick_align(seqs, pairs):
+    """Quick k-tuple distances (float64) from the oracle: the sharded path must
+    keep them bit for bit."""
+    from oracle import oracle
+
+    fp = dict(dna=0, ktup=1, window=5, window_gap=3, signif=5, percent=1, max_aa=24,
+              max_aln_length=2 * max(len(s) for s in seqs))
+    return oracle.fast_pairs(seqs, fp, pairs, nthreads=1)["dist"]
+
+
+def _rank_main_quick(rank, world, port, out_path):
+    import sys
+
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    here = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    sys.path.insert(0, here)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from clustalw_gb300.shard import sharded_pairwise
+    from clustalw_gb300.synth import all_pairs, protein_family
+
+    seqs = protein_family(14, 120, 3)
+    res = sharded_pairwise(seqs, all_pairs(len(seqs)), quick_align, group=dist.group.WORLD)
+    if rank == 0:
+        np.save(out_path, res)
+    dist.destroy_process_group()
+
+
+def test_two_gloo_ranks_keep_quick_distances_exact(tmp_path):
+    import socket
+
+    from clustalw_gb300.synth import all_pairs, protein_family
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = str(tmp_path / "q.npy")
+    mp.spawn(_rank_main_quick, args=(2, port, out), nprocs=2, join=True)
+    seqs = protein_family(14, 120, 3)
+    want = quick_align(seqs, all_pairs(len(seqs)))
+    got = np.load(out)
+    assert got.dtype == np.float64
+    assert np.array_equal(got.view(np.int64), want.view(np.int64))
