@@ -493,22 +493,27 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ int s_mini, s_minj, s_repi, s_repj;
     __shared__ double s_sR, s_sC, s_sumd, s_dio, s_djo, s_avi, s_avj, s_dmin;
-    if (warp == 0) {
+    Cand b;
+    {
+        // Every CTA's candidate, one per thread of this CTA (all loads in one
+        // round trip), reduced per warp and then across the warps.
+        __shared__ Cand s_cand[kWarps];
         const double f = __ldcg(A.scal + 1);
-        Cand b{okey(__dmul_rn(__dmul_rn(99999.0, 2.0), f)), -1, make_int2(0, 0), 0.0};
-        // All loads first (the grid is at most kMaxGrid CTAs), then the minimum.
-        Cand o[kMaxGrid / 32];
-#pragma unroll
-        for (int q = 0; q < kMaxGrid / 32; ++q) {
-            const int k = lane + 32 * q;
-            o[q] = b;
-            if (k < (int)gridDim.x)
-                o[q] = Cand{__ldcg(A.cand_k + k), __ldcg(A.cand_idx + k), __ldcg(A.cand_ij + k), __ldcg(A.cand_d + k)};
+        const Cand none{okey(__dmul_rn(__dmul_rn(99999.0, 2.0), f)), -1, make_int2(0, 0), 0.0};
+        b = none;
+        for (int k = threadIdx.x; k < (int)gridDim.x; k += blockDim.x) {
+            const Cand o{__ldcg(A.cand_k + k), __ldcg(A.cand_idx + k), __ldcg(A.cand_ij + k), __ldcg(A.cand_d + k)};
+            if (better(o.k, o.i, b.k, b.i)) b = o;
         }
-#pragma unroll
-        for (int q = 0; q < kMaxGrid / 32; ++q)
-            if (better(o[q].k, o[q].i, b.k, b.i)) b = o[q];
         warp_min(b);
+        if (lane == 0) s_cand[warp] = b;
+        __syncthreads();
+        if (warp == 0) {
+            b = lane < kWarps ? s_cand[lane] : none;
+            warp_min(b);
+        }
+    }
+    if (warp == 0) {
         if (lane == 0) {
             const int mi = b.i >= 0 ? b.ij.x : 0, mj = b.i >= 0 ? b.ij.y : 0;
             s_mini = mi;
