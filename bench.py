@@ -671,7 +671,7 @@ def ours_arm(args):
             "batched_over_plain": value / world / plain_gcups,
         },
         "roofline": roofline,
-        "gpu_launches": args.steps,
+        "gpu_launches": args.steps * plan.kernel_count(),
     }
     if rank == 0:
         clocks = clk.summary()

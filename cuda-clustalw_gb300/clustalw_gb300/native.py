@@ -147,6 +147,7 @@ SIGNATURES = {
     "cwgpu_plan_results": (ctypes.c_int, [_vp, _vp, _vp]),
     "cwgpu_plan_device_dist": (_vp, [_vp]),
     "cwgpu_plan_cell_counts": (ctypes.c_int, [_vp, _vp]),
+    "cwgpu_plan_kernel_count": (ctypes.c_int, [_vp]),
     "cwgpu_plan_destroy": (None, [_vp]),
     "cwgpu_synchronize": (ctypes.c_int, [_vp]),
     "cwgpu_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
@@ -379,6 +380,10 @@ class Plan:
         c = np.zeros(3, dtype=np.int64)
         self.ctx._check(self._lib.cwgpu_plan_cell_counts(self._h, _ptr(c)), "cwgpu_plan_cell_counts")
         return tuple(int(x) for x in c)
+
+    def kernel_count(self):
+        """Kernels one launch of this plan runs (long-pair and/or short-pair)."""
+        return int(self._lib.cwgpu_plan_kernel_count(self._h))
 
     def device_dist_ptr(self):
         return self._lib.cwgpu_plan_device_dist(self._h)

@@ -29,8 +29,13 @@
 namespace {
 
 constexpr int kWarpsPerBlock = 4;  // warps (= concurrent pairs) per CTA
+constexpr int kCounterWords = 8;   // cwgpu_context::d_counter
 
-__global__ void __launch_bounds__(kWarpsPerBlock * 32)
+// RS = rows per lane of every sweep: cwgpu::kR for the long-pair kernel,
+// cwgpu::kRShort for pairs whose first sequence has at most kShortRows
+// residues. Separate kernels keep the long-pair code exactly as tuned.
+template <int RS>
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, RS == cwgpu::kR ? 0 : 5)
     k_pairwise(cwgpu::PairArgs g, long long single) {
     __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
     extern __shared__ __align__(16) uint16_t region_all[];
@@ -52,14 +57,14 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32)
     int2* bufB = bufA + (g.lmax + 1);
     unsigned long long acc[3] = {0, 0, 0};
     if (single >= 0) {
-        if (slot == 0) cwgpu::align_pair(g, single, X, bufA, bufB, acc);
+        if (slot == 0) cwgpu::align_pair<RS>(g, single, X, bufA, bufB, acc);
     } else {
         for (;;) {
             unsigned long long k = 0;
             if (lane == 0) k = atomicAdd(g.counter, 1ULL);
             k = __shfl_sync(cwgpu::kFull, k, 0);
             if (k >= (unsigned long long)g.npairs) break;
-            cwgpu::align_pair(g, (long long)g.order[k], X, bufA, bufB, acc);
+            cwgpu::align_pair<RS>(g, (long long)g.order[k], X, bufA, bufB, acc);
         }
     }
     if (lane == 0 && g.cells && (acc[0] | acc[1] | acc[2])) {
@@ -80,9 +85,12 @@ struct cwgpu_plan {
     int32_t* d_order = nullptr;
     float* d_dist = nullptr;
     cwgpu_pair_stats* d_stats = nullptr;
+    int64_t nlong = 0;  // order[0, nlong): long-pair kernel; order[nlong, npairs): short-pair kernel
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
+    cudaStream_t fork_stream = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
     unsigned generation = 0;
 };
 
@@ -158,21 +166,38 @@ int gap_extend_of(const cwgpu_params& p) {
 
 size_t block_smem(int K, int warps) { return (size_t)cwgpu::warp_region_bytes(K) * warps; }
 
-// Persistent grid: as many CTAs as fit on every SM at once.
+template <int RS>
+int persistent_grid(cwgpu_context* ctx, int* grid) {
+    int per_sm = 0;
+    const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
+    CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise<RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)block_smem(CWGPU_NUMRES, kWarpsPerBlock)));
+    CW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise<RS>, kWarpsPerBlock * 32, smem));
+    *grid = (per_sm < 1 ? 1 : per_sm) * ctx->sm_count;
+    return CWGPU_OK;
+}
+
+bool has_short_seqs(const cwgpu_context* ctx) {
+    for (int s = 0; s < ctx->nseqs; ++s)
+        if (ctx->lens[s] <= cwgpu::kShortRows) return true;
+    return false;
+}
+
+// Persistent grids: as many CTAs as fit on every SM at once, per kernel. The
+// scratch holds one (bufA, bufB) pair per warp slot of the long-pair grid,
+// followed by the short-pair grid's slots when the set has short sequences
+// (the two kernels of a plan can run at the same time).
 int ensure_scratch(cwgpu_context* ctx) {
     if (ctx->grid == 0 || ctx->grid_K != ctx->K) {
-        int per_sm = 0;
-        const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
-        CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                          (int)block_smem(CWGPU_NUMRES, kWarpsPerBlock)));
-        CW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise, kWarpsPerBlock * 32, smem));
-        if (per_sm < 1) per_sm = 1;
-        ctx->grid = per_sm * ctx->sm_count;
+        int rc = persistent_grid<cwgpu::kR>(ctx, &ctx->grid);
+        if (!rc) rc = persistent_grid<cwgpu::kRShort>(ctx, &ctx->grid_short);
+        if (rc) return rc;
         ctx->grid_K = ctx->K;
         ctx->scratch_bytes = 0;  // grid changed: resize below
         dfree(ctx->d_scratch);
     }
-    const size_t need = (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1) * sizeof(int2);
+    const int64_t slots = (int64_t)(ctx->grid + (has_short_seqs(ctx) ? ctx->grid_short : 0)) * kWarpsPerBlock;
+    const size_t need = (size_t)slots * 2 * (size_t)(ctx->lmax + 1) * sizeof(int2);
     if (need > ctx->scratch_bytes) {
         dfree(ctx->d_scratch);
         ctx->scratch_bytes = 0;
@@ -232,15 +257,46 @@ int validate_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs) {
     return CWGPU_OK;
 }
 
-// Longest pairs first, so the tail of the persistent queue holds short work.
-std::vector<int32_t> work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs) {
+bool short_pair(const cwgpu_context* ctx, const int32_t* pairs, int64_t q) {
+    return ctx->lens[pairs[2 * q]] <= cwgpu::kShortRows;
+}
+
+// Pairs for the long-pair kernel first, then those for the short-pair kernel
+// (*nlong of them are long); each part longest first, so the tail of each
+// persistent queue holds its shortest work.
+std::vector<int32_t> work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, int64_t* nlong) {
     std::vector<int32_t> order((size_t)npairs);
     std::iota(order.begin(), order.end(), 0);
     std::vector<int64_t> work((size_t)npairs);
     for (int64_t q = 0; q < npairs; ++q)
         work[q] = (int64_t)ctx->lens[pairs[2 * q]] * (int64_t)ctx->lens[pairs[2 * q + 1]];
-    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) { return work[x] > work[y]; });
+    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
+        const bool sx = short_pair(ctx, pairs, x), sy = short_pair(ctx, pairs, y);
+        if (sx != sy) return sy;
+        return work[x] > work[y];
+    });
+    int64_t k = 0;
+    while (k < npairs && !short_pair(ctx, pairs, order[k])) ++k;
+    *nlong = k;
     return order;
+}
+
+// One persistent launch of k_pairwise<RS> over g's queue with a kernel-node
+// priority (honoured by graphs instantiated with UseNodePriority).
+template <int RS>
+cudaError_t launch_persistent(const cwgpu::PairArgs& g, int max_grid, size_t smem, int priority, cudaStream_t s) {
+    const int grid = (int)std::min<int64_t>(max_grid, (g.npairs + kWarpsPerBlock - 1) / kWarpsPerBlock);
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(kWarpsPerBlock * 32);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = priority;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_pairwise<RS>, g, -1LL);
 }
 
 int check_kernel_error(cwgpu_context* ctx) {
@@ -314,8 +370,8 @@ int cwgpu_create(int device, cwgpu_context** out) {
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, 4 * sizeof(unsigned long long));
-    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, 4 * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, kCounterWords * sizeof(unsigned long long));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_matrix, sizeof(int32_t) * CWGPU_NUMRES * CWGPU_NUMRES);
@@ -453,25 +509,50 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
     if (e == cudaSuccess) e = cudaMalloc(&p->d_dist, sizeof(float) * np);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_stats, sizeof(cwgpu_pair_stats) * np);
     if (e == cudaSuccess && npairs > 0) {
-        std::vector<int32_t> order = work_order(ctx, pairs, npairs);
+        std::vector<int32_t> order = work_order(ctx, pairs, npairs, &p->nlong);
         e = cudaMemcpy(p->d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(p->d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) {
-        // Capture: reset the queue counter, then one persistent launch.
-        cwgpu::PairArgs g = make_args(ctx, p->d_pairs, p->d_order, npairs, p->d_dist, p->d_stats);
+        // Capture: reset the queue counters, then one persistent launch per
+        // kernel. With both kinds of pairs the short-pair kernel runs beside
+        // the long-pair one at lower priority, so its CTAs take the SM slots
+        // that long-pair CTAs leave as the long queue drains.
+        const int64_t nshort = npairs - p->nlong;
+        cwgpu::PairArgs gl = make_args(ctx, p->d_pairs, p->d_order, p->nlong, p->d_dist, p->d_stats);
+        cwgpu::PairArgs gs = make_args(ctx, p->d_pairs, p->d_order + p->nlong, nshort, p->d_dist, p->d_stats);
+        gs.counter = ctx->d_counter + 4;
+        if (p->nlong > 0) gs.scratch += (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1);
         const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
-        e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
+        const bool both = p->nlong > 0 && nshort > 0;
+        int prio_low = 0, prio_high = 0;
+        e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess && both) e = cudaStreamCreateWithFlags(&p->fork_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess && both) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
+        if (e == cudaSuccess && both) e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaMemsetAsync(ctx->d_counter, 0, 4 * sizeof(unsigned long long), p->graph_stream);
-            if (npairs > 0) {
-                const int grid = (int)std::min<int64_t>(ctx->grid, (npairs + kWarpsPerBlock - 1) / kWarpsPerBlock);
-                k_pairwise<<<grid, kWarpsPerBlock * 32, smem, p->graph_stream>>>(g, -1);
+            cudaError_t ce = cudaMemsetAsync(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long),
+                                             p->graph_stream);
+            cudaStream_t short_stream = p->graph_stream;
+            if (ce == cudaSuccess && both) {
+                ce = cudaEventRecord(p->fork, p->graph_stream);
+                if (ce == cudaSuccess) ce = cudaStreamWaitEvent(p->fork_stream, p->fork, 0);
+                short_stream = p->fork_stream;
+            }
+            if (ce == cudaSuccess && p->nlong > 0)
+                ce = launch_persistent<cwgpu::kR>(gl, ctx->grid, smem, prio_high, p->graph_stream);
+            if (ce == cudaSuccess && nshort > 0)
+                ce = launch_persistent<cwgpu::kRShort>(gs, ctx->grid_short, smem, prio_low, short_stream);
+            if (ce == cudaSuccess && both) {
+                ce = cudaEventRecord(p->join, p->fork_stream);
+                if (ce == cudaSuccess) ce = cudaStreamWaitEvent(p->graph_stream, p->join, 0);
             }
             e = cudaStreamEndCapture(p->graph_stream, &p->graph);
+            if (e == cudaSuccess) e = ce;
         }
-        if (e == cudaSuccess) e = cudaGraphInstantiate(&p->exec, p->graph, 0);
+        if (e == cudaSuccess) e = cudaGraphInstantiateWithFlags(&p->exec, p->graph, cudaGraphInstantiateFlagUseNodePriority);
     }
     if (e != cudaSuccess) {
         cwgpu_plan_destroy(p);
@@ -520,6 +601,11 @@ int cwgpu_plan_cell_counts(cwgpu_plan* p, int64_t* counts) {
     return CWGPU_OK;
 }
 
+int cwgpu_plan_kernel_count(const cwgpu_plan* p) {
+    if (!p) return 0;
+    return (p->nlong > 0 ? 1 : 0) + (p->npairs > p->nlong ? 1 : 0);
+}
+
 void cwgpu_plan_destroy(cwgpu_plan* p) {
     if (!p) return;
     if (p->ctx) cudaSetDevice(p->ctx->device);
@@ -527,6 +613,9 @@ void cwgpu_plan_destroy(cwgpu_plan* p) {
     if (p->exec) cudaGraphExecDestroy(p->exec);
     if (p->graph) cudaGraphDestroy(p->graph);
     if (p->graph_stream) cudaStreamDestroy(p->graph_stream);
+    if (p->fork_stream) cudaStreamDestroy(p->fork_stream);
+    if (p->fork) cudaEventDestroy(p->fork);
+    if (p->join) cudaEventDestroy(p->join);
     dfree(p->d_pairs);
     dfree(p->d_order);
     dfree(p->d_dist);
@@ -561,11 +650,14 @@ int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t np
     if (e == cudaSuccess) e = cudaMalloc(&d_dist, sizeof(float) * npairs);
     if (e == cudaSuccess) e = cudaMalloc(&d_stats, sizeof(cwgpu_pair_stats) * npairs);
     if (e == cudaSuccess) e = cudaMemcpy(d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counter, 0, 4 * sizeof(unsigned long long), ctx->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long), ctx->stream);
     if (e == cudaSuccess) {
         cwgpu::PairArgs g = make_args(ctx, d_pairs, nullptr, npairs, d_dist, d_stats);
         for (int64_t q = 0; q < npairs && e == cudaSuccess; ++q) {
-            k_pairwise<<<1, 32, block_smem(ctx->K, 1), ctx->stream>>>(g, (long long)q);
+            if (short_pair(ctx, pairs, q))
+                k_pairwise<cwgpu::kRShort><<<1, 32, block_smem(ctx->K, 1), ctx->stream>>>(g, (long long)q);
+            else
+                k_pairwise<cwgpu::kR><<<1, 32, block_smem(ctx->K, 1), ctx->stream>>>(g, (long long)q);
             e = cudaGetLastError();
         }
     }

@@ -40,9 +40,10 @@ struct cwgpu_context {
     int go_len = 0;
     int2* d_scratch = nullptr;
     size_t scratch_bytes = 0;
-    unsigned long long* d_counter = nullptr;  // [0] queue head, [1..3] cell counts
+    unsigned long long* d_counter = nullptr;  // [0] queue head, [1..3] cell counts, [4] short-pair queue head
     int* d_err = nullptr;
-    int grid = 0;
+    int grid = 0;        // persistent CTAs of the long-pair kernel
+    int grid_short = 0;  // and of the short-pair kernel
     int grid_K = -1;  // K the grid size was computed for
     bool derived_dirty = true;
     unsigned generation = 0;  // bumped whenever device inputs or scratch move

@@ -25,7 +25,8 @@
 // which is the reference's recurrence written with fewer operations.
 //
 // Scores come from a per-stripe int16 profile in shared memory,
-// prof[code][lane][row], one conflict-free 16-byte load per step and lane.
+// prof[code][lane][row], one conflict-free 16-byte load per step and lane
+// (8 bytes in the short-pair kernel, whose lanes hold 4 rows).
 // Residues are remapped on the host to the K codes that occur (K <= 32), so
 // the profile holds K rows of codes.
 //
@@ -43,7 +44,9 @@
 namespace cwgpu {
 
 constexpr unsigned kFull = 0xffffffffu;
-constexpr int kR = 8;              // rows per lane in every sweep
+constexpr int kR = 8;              // rows per lane in every sweep of long pairs
+constexpr int kRShort = 4;         // rows per lane in the short-pair kernel
+constexpr int kShortRows = 32 * kRShort;  // pairs whose first sequence fits one 4-row stripe
 constexpr int kTinyMaxN = 16;      // tiny frames: N <= kTinyMaxN (shared-memory rows)
 constexpr int kTinyStride = kTinyMaxN + 1;
 constexpr int kTinyWords = 4 * kTinyStride * 32;  // HH, DD, RR, SS for 32 lanes
@@ -100,33 +103,53 @@ struct SweepState {
     int ch, ce, nh, ne;  // boundary chunks: current and next W columns
 };
 
-__device__ __forceinline__ void unpack8(uint4 w, int (&s)[8]) {
-    s[0] = (int)(int16_t)(w.x & 0xffffu);
-    s[1] = ((int)w.x) >> 16;
-    s[2] = (int)(int16_t)(w.y & 0xffffu);
-    s[3] = ((int)w.y) >> 16;
-    s[4] = (int)(int16_t)(w.z & 0xffffu);
-    s[5] = ((int)w.z) >> 16;
-    s[6] = (int)(int16_t)(w.w & 0xffffu);
-    s[7] = ((int)w.w) >> 16;
+__device__ __forceinline__ void unpack2(unsigned w, int& lo, int& hi) {
+    lo = (int)(int16_t)(w & 0xffffu);
+    hi = ((int)w) >> 16;
+}
+
+// The R int16 scores of one (code, lane) profile entry: one 16-byte (R == 8)
+// or 8-byte (R == 4) shared load.
+template <int R>
+__device__ __forceinline__ void load_scores(const uint16_t* p, int (&s)[R]) {
+    static_assert(R == 8 || R == 4, "profile entries hold 4 or 8 rows");
+    if constexpr (R == 8) {
+        const uint4 w = *reinterpret_cast<const uint4*>(p);
+        unpack2(w.x, s[0], s[1]);
+        unpack2(w.y, s[2], s[3]);
+        unpack2(w.z, s[4], s[5]);
+        unpack2(w.w, s[6], s[7]);
+    } else {
+        const uint2 w = *reinterpret_cast<const uint2*>(p);
+        unpack2(w.x, s[0], s[1]);
+        unpack2(w.y, s[2], s[3]);
+    }
 }
 
 __device__ __forceinline__ unsigned pack2(int lo, int hi) {
     return ((unsigned)lo & 0xffffu) | ((unsigned)hi << 16);
 }
 
-// prof[(b*32 + lane)*8 + k] = matrix[a[k]][b] for the K codes b. Lane l starts
+// prof[(b*32 + lane)*R + k] = matrix[a[k]][b] for the K codes b. Lane l starts
 // at code l % K so that its shared-matrix reads spread over the banks.
-__device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, const int (&a)[8], int lane,
+template <int R>
+__device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, const int (&a)[R], int lane,
                                               int K) {
     int b = lane % K;
     for (int i = 0; i < K; ++i) {
-        uint4 w;
-        w.x = pack2(smat[a[0] * 32 + b], smat[a[1] * 32 + b]);
-        w.y = pack2(smat[a[2] * 32 + b], smat[a[3] * 32 + b]);
-        w.z = pack2(smat[a[4] * 32 + b], smat[a[5] * 32 + b]);
-        w.w = pack2(smat[a[6] * 32 + b], smat[a[7] * 32 + b]);
-        *reinterpret_cast<uint4*>(prof + (b * 32 + lane) * 8) = w;
+        if constexpr (R == 8) {
+            uint4 w;
+            w.x = pack2(smat[a[0] * 32 + b], smat[a[1] * 32 + b]);
+            w.y = pack2(smat[a[2] * 32 + b], smat[a[3] * 32 + b]);
+            w.z = pack2(smat[a[4] * 32 + b], smat[a[5] * 32 + b]);
+            w.w = pack2(smat[a[6] * 32 + b], smat[a[7] * 32 + b]);
+            *reinterpret_cast<uint4*>(prof + (b * 32 + lane) * 8) = w;
+        } else {
+            uint2 w;
+            w.x = pack2(smat[a[0] * 32 + b], smat[a[1] * 32 + b]);
+            w.y = pack2(smat[a[2] * 32 + b], smat[a[3] * 32 + b]);
+            *reinterpret_cast<uint2*>(prof + (b * 32 + lane) * 4) = w;
+        }
         b = (b + 1 == K) ? 0 : b + 1;
     }
 }
@@ -171,7 +194,7 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
         S.bnext = (int)__ldg(T.cseq + min(max(c, 0), cmax) * T.cdir);  // next step's column, clamped in range
         if ((unsigned)(c - 1) < (unsigned)T.cols) {
             int sc[R];
-            unpack8(*reinterpret_cast<const uint4*>(prof_lane + b * (32 * R)), sc);
+            load_scores<R>(prof_lane + b * (32 * R), sc);
             int hup = hin, eup = ein, d = S.diag;
             int hs[R];
 #pragma unroll
@@ -233,7 +256,6 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
 // examined one by one.
 template <int R, int W, int MODE>
 __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, Best& best) {
-    static_assert(R == 8, "profile layout written for R == 8");
     const int lane = threadIdx.x & 31;
     const int sl = lane & (W - 1);
     const int goe = go + ge;
@@ -261,7 +283,7 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, B
 #pragma unroll
         for (int k = 0; k < R; ++k) a[k] = (k < nvalid) ? (int)__ldg(T.rseq + (lrow0 + k) * T.rdir) : 0;
         __syncwarp();  // previous users of the shared region are done
-        build_profile(X.region, X.smat, a, lane, X.K);
+        build_profile<R>(X.region, X.smat, a, lane, X.K);
         __syncwarp();  // previous stripe's buf writes visible to the whole segment
 
         const int gbest = best.val;
@@ -478,6 +500,7 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
 // free; the top frame's score is diff()'s return value. tb/te are always 0 or
 // gapOpen, kept as flags. s1/s2 are 0-based: the reference's 1-based residue
 // seq1[A + i] is s1[A + i - 1].
+template <int RS>
 static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int go, int ge,
                          int2* bufA, int2* bufB, const Env& X, int& mm_score, int& n_ident, int& n_match,
                          long long& cells) {
@@ -607,7 +630,7 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int 
         t.hls = ge;
         t.fo = go;
         Best unused;
-        sweep<kR, 16, MODE_GLOBAL>(t, go, ge, 0, X, unused);
+        sweep<RS, 16, MODE_GLOBAL>(t, go, ge, 0, X, unused);
 
         // Midpoint scans (:570-593). Scan 1 keeps the first j reaching the
         // maximum of HH+RR, replaced by the last tied j with HH!=DD && RR==SS;
@@ -729,7 +752,11 @@ struct PairArgs {
 // forwardPass + reversePass + diff + distance for one pair, given its 0-based
 // code pointers, lengths, non-gap residue counts and gap penalties. Returns
 // the distance and fills `st`; adds the algorithmic cell counts (the
-// inner-loop iterations the reference executes) to acc[0..2].
+// inner-loop iterations the reference executes) to acc[0..2]. RS = rows per
+// lane in every sweep: any RS gives the same results; kRShort needs fewer
+// steps when n <= kShortRows (one stripe, lanes of 4 rows instead of
+// half-empty lanes of 8).
+template <int RS = kR>
 static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int m, int len1, int len2, int go, int ge,
                            int2* bufA, int2* bufB, const Env& X, cwgpu_pair_stats& st, unsigned long long (&acc)[3]) {
     st = cwgpu_pair_stats{0, 0, 0, 0, 0, 0, 0, 0};
@@ -750,7 +777,7 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
     t.fo = go;
     t.buf = bufA;
     Best fb;
-    sweep<kR, 32, MODE_LOCAL_FWD>(t, go, ge, 0, X, fb);
+    sweep<RS, 32, MODE_LOCAL_FWD>(t, go, ge, 0, X, fb);
     const int max_score = fb.val;
     const int se1 = max_score > 0 ? (int)(fb.key >> 16) + 1 : 0;
     const int se2 = max_score > 0 ? (int)(fb.key & 0xffffu) : 0;
@@ -773,7 +800,7 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
         r.fo = 0;
         r.buf = bufA;
         Best rb;
-        sweep<kR, 32, MODE_LOCAL_REV>(r, go, ge, max_score, X, rb);
+        sweep<RS, 32, MODE_LOCAL_REV>(r, go, ge, max_score, X, rb);
         if (rb.val > 0) {
             sb1 = se1 - (int)(rb.key >> 16);
             sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
@@ -789,7 +816,7 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
     // diff + tracePath
     int mm = 0, ident = 0, matches = 0;
     long long dcells = 0;
-    mm_align(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, bufA, bufB, X, mm, ident, matches,
+    mm_align<RS>(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, bufA, bufB, X, mm, ident, matches,
              dcells);
     acc[2] += (unsigned long long)dcells;
 
@@ -811,13 +838,14 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
 }
 
 // Aligns pair q: FullPairwiseAlign.cpp:112-183 for one (si, sj).
+template <int RS = kR>
 static __device__ void align_pair(const PairArgs& g, long long q, const Env& X, int2* bufA, int2* bufB,
                            unsigned long long (&acc)[3]) {
     const int lane = threadIdx.x & 31;
     const int si = g.pairs[2 * q], sj = g.pairs[2 * q + 1];
     const int n = g.lens[si], m = g.lens[sj];
     cwgpu_pair_stats st;
-    const float dist = align_one(g.codes + g.offs[si], n, g.codes + g.offs[sj], m, g.nres[si], g.nres[sj],
+    const float dist = align_one<RS>(g.codes + g.offs[si], n, g.codes + g.offs[sj], m, g.nres[si], g.nres[sj],
                                  g.go_table[min(n, m)], g.ge, bufA, bufB, X, st, acc);
     if (lane == 0) {
         g.dist[q] = dist;

@@ -142,7 +142,9 @@ int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t np
  * A plan uploads a pair list and its load-balancing order (longest pairs
  * first) once, owns device output arrays and holds a CUDA graph of the
  * persistent launch, so repeated runs over resident inputs cost one
- * cudaGraphLaunch. A plan is tied to the sequences, matrix and params that were
+ * cudaGraphLaunch. Pairs whose first sequence has at most 128 residues run in
+ * a second persistent kernel (4 rows per lane instead of 8) inside the same
+ * graph, beside the long-pair kernel at lower priority. A plan is tied to the sequences, matrix and params that were
  * current when it was made: after cwgpu_upload_seqs/set_params/set_matrix,
  * cwgpu_plan_launch returns CWGPU_ERR_STATE. Plans of one context share its
  * scratch memory and must not run concurrently. No reference counterpart: the
@@ -161,6 +163,8 @@ void* cwgpu_plan_device_dist(cwgpu_plan* plan);
  * (:351-414), counts[2] diff() inner-loop iterations (:450-566). These are the
  * iteration counts the reference itself executes for the same pairs. */
 int cwgpu_plan_cell_counts(cwgpu_plan* plan, int64_t* counts);
+/* Kernels one cwgpu_plan_launch runs (0, 1 or 2: long-pair and short-pair). */
+int cwgpu_plan_kernel_count(const cwgpu_plan* plan);
 void cwgpu_plan_destroy(cwgpu_plan* plan);
 
 /* ---- allocation-free variant ---------------------------------------------

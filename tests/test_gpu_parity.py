@@ -103,3 +103,44 @@ def test_cell_counts_match_oracle(ctx, oracle_mod, name):
     plan.close()
     want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
     assert (fwd, rev, dif) == (int(want["cells_fwd"].sum()), int(want["cells_rev"].sum()), int(want["cells_diff"].sum()))
+
+
+def test_short_and_long_pair_kernels_at_the_boundary(ctx, oracle_mod):
+    """Pairs whose first sequence has <= 128 residues run in the 4-rows-per-lane
+    kernel, the rest in the 8-row kernel, both inside one plan. Lengths around
+    the 128-row split and the 32/64-row stripe edges, in both pair orders,
+    must match the oracle field for field."""
+    from clustalw_gb300 import load_matrix, synth
+
+    matrix, params = load_matrix("protein")
+    base = synth.protein_family(16, 300, seed=11)
+    lens = [1, 2, 31, 32, 33, 63, 64, 65, 127, 128, 129, 130, 255, 256, 257, 300]
+    seqs = [s[:L] if len(s) >= L else np.concatenate([s, s])[:L] for s, L in zip(base, lens)]
+    ctx.set_matrix(matrix)
+    ctx.set_params(params)
+    ctx.upload_seqs(seqs)
+    pairs = range_pairs(len(seqs), 0, len(seqs), 0, len(seqs))
+    pairs = np.concatenate([pairs, pairs[:, ::-1]]).astype(np.int32)
+    plan = ctx.plan(pairs)
+    assert plan.kernel_count() == 2
+    plan.launch()
+    dist, st = plan.results(stats=True)
+    fwd, rev, dif = plan.cell_counts()
+    plan.close()
+    want = oracle_mod.align_pairs(seqs, matrix, params, pairs)
+    assert np.array_equal(dist.view(np.int32), want["dist"].view(np.int32))
+    for f in STAT_FIELDS:
+        bad = np.nonzero(st[f] != want[f])[0]
+        assert len(bad) == 0, f"{f}: pair {pairs[bad[0]]} gpu {st[f][bad[0]]} oracle {want[f][bad[0]]}"
+    assert (fwd, rev, dif) == (int(want["cells_fwd"].sum()), int(want["cells_rev"].sum()), int(want["cells_diff"].sum()))
+    d_plain, s_plain = ctx.align_pairs(pairs, stats=True, plain=True)
+    assert np.array_equal(d_plain, dist) and np.array_equal(s_plain, st)
+
+
+@pytest.mark.parametrize("name,kernels", [("fixture_100_97", 1), ("fixture_100_498", 1), ("synth_uneven_40", 2)])
+def test_plan_kernel_count(ctx, name, kernels):
+    g = load_golden(name)
+    setup(ctx, g)
+    plan = ctx.plan(range_pairs(len(g["seqs"]), *g["range"]))
+    assert plan.kernel_count() == kernels
+    plan.close()
