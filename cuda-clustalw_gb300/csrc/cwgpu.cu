@@ -118,6 +118,19 @@ void dfree(T*& p) {
     p = nullptr;
 }
 
+// Grow-only device array: reallocates (contents lost) only when `need`
+// elements exceed the capacity.
+template <class T>
+cudaError_t grow(T*& p, int64_t& cap, int64_t need) {
+    if (need <= cap && p) return cudaSuccess;
+    dfree(p);
+    cap = 0;
+    const int64_t n = std::max<int64_t>(need, 1);
+    cudaError_t e = cudaMalloc(&p, sizeof(T) * (size_t)n);
+    if (e == cudaSuccess) cap = n;
+    return e;
+}
+
 // Recomputes nres and the gap-open table after sequences or params changed.
 int refresh_derived(cwgpu_context* ctx) {
     if (!ctx->derived_dirty) return CWGPU_OK;
@@ -131,8 +144,6 @@ int refresh_derived(cwgpu_context* ctx) {
             if (p[i] != ctx->params.gap_pos1 && p[i] != ctx->params.gap_pos2) ++c;
         nres[s] = c;
     }
-    dfree(ctx->d_nres);
-    CW_CUDA(ctx, cudaMalloc(&ctx->d_nres, sizeof(int32_t) * std::max(1, ctx->nseqs)));
     if (ctx->nseqs)
         CW_CUDA(ctx, cudaMemcpy(ctx->d_nres, nres.data(), sizeof(int32_t) * ctx->nseqs, cudaMemcpyHostToDevice));
     std::vector<int32_t> go(ctx->lmax + 1);
@@ -141,8 +152,7 @@ int refresh_derived(cwgpu_context* ctx) {
         cwgpu_gap_penalties(&ctx->params, L, L, &g, &e);
         go[L] = g;
     }
-    dfree(ctx->d_go);
-    CW_CUDA(ctx, cudaMalloc(&ctx->d_go, sizeof(int32_t) * go.size()));
+    CW_CUDA(ctx, grow(ctx->d_go, ctx->cap_go, (int64_t)go.size()));
     CW_CUDA(ctx, cudaMemcpy(ctx->d_go, go.data(), sizeof(int32_t) * go.size(), cudaMemcpyHostToDevice));
     ctx->go_len = (int)go.size();
     // Matrix over the dense codes, row stride 32 (entries past K unused).
@@ -262,22 +272,27 @@ bool short_pair(const cwgpu_context* ctx, const int32_t* pairs, int64_t q) {
 }
 
 // Pairs for the long-pair kernel first, then those for the short-pair kernel
-// (*nlong of them are long); each part longest first, so the tail of each
-// persistent queue holds its shortest work.
+// (*nlong of them are long); each part longest first (by n*m), so the tail of
+// each persistent queue holds its shortest work. The order only balances the
+// load, so a counting sort on a coarse key does: the top 12 bits of n*m as a
+// float (exponent and 4 mantissa bits, 1/16 relative resolution), stable.
 std::vector<int32_t> work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, int64_t* nlong) {
+    constexpr int kKeyBits = 12, kBuckets = 1 << kKeyBits;
+    std::vector<uint16_t> key((size_t)npairs);
+    std::vector<int64_t> start(2 * kBuckets + 1, 0);
+    for (int64_t q = 0; q < npairs; ++q) {
+        const float w = (float)((double)ctx->lens[pairs[2 * q]] * (double)ctx->lens[pairs[2 * q + 1]]);
+        uint32_t bits;
+        memcpy(&bits, &w, sizeof(bits));  // w >= 0: the bit pattern grows with w
+        const int b = (int)(bits >> (31 - kKeyBits));
+        const int k = (short_pair(ctx, pairs, q) ? kBuckets : 0) + (kBuckets - 1 - b);
+        key[(size_t)q] = (uint16_t)k;
+        ++start[k + 1];
+    }
+    for (int k = 0; k < 2 * kBuckets; ++k) start[k + 1] += start[k];
+    *nlong = start[kBuckets];
     std::vector<int32_t> order((size_t)npairs);
-    std::iota(order.begin(), order.end(), 0);
-    std::vector<int64_t> work((size_t)npairs);
-    for (int64_t q = 0; q < npairs; ++q)
-        work[q] = (int64_t)ctx->lens[pairs[2 * q]] * (int64_t)ctx->lens[pairs[2 * q + 1]];
-    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-        const bool sx = short_pair(ctx, pairs, x), sy = short_pair(ctx, pairs, y);
-        if (sx != sy) return sy;
-        return work[x] > work[y];
-    });
-    int64_t k = 0;
-    while (k < npairs && !short_pair(ctx, pairs, order[k])) ++k;
-    *nlong = k;
+    for (int64_t q = 0; q < npairs; ++q) order[(size_t)start[key[(size_t)q]]++] = (int32_t)q;
     return order;
 }
 
@@ -297,6 +312,41 @@ cudaError_t launch_persistent(const cwgpu::PairArgs& g, int max_grid, size_t sme
     cfg.attrs = attr;
     cfg.numAttrs = 1;
     return cudaLaunchKernelEx(&cfg, k_pairwise<RS>, g, -1LL);
+}
+
+// The queue-counter reset and one persistent launch per kernel: long pairs
+// on s, short pairs on s2 forked from s when both kinds are present (joined
+// back into s), else on s. The short-pair kernel runs at lower priority so
+// that its CTAs take the SM slots long-pair CTAs leave as the long queue
+// drains. Works the same under stream capture.
+cudaError_t enqueue_pairs(cwgpu_context* ctx, const cwgpu::PairArgs& gl, const cwgpu::PairArgs& gs, cudaStream_t s,
+                          cudaStream_t s2, cudaEvent_t fork, cudaEvent_t join) {
+    const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
+    const bool both = gl.npairs > 0 && gs.npairs > 0;
+    cudaError_t e = cudaMemsetAsync(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long), s);
+    cudaStream_t short_stream = s;
+    if (e == cudaSuccess && both) {
+        e = cudaEventRecord(fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
+        short_stream = s2;
+    }
+    if (e == cudaSuccess && gl.npairs > 0) e = launch_persistent<cwgpu::kR>(gl, ctx->grid, smem, ctx->prio_high, s);
+    if (e == cudaSuccess && gs.npairs > 0)
+        e = launch_persistent<cwgpu::kRShort>(gs, ctx->grid_short, smem, ctx->prio_low, short_stream);
+    if (e == cudaSuccess && both) {
+        e = cudaEventRecord(join, s2);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    }
+    return e;
+}
+
+// Arguments of the two kernels over one ordered pair list (long pairs first).
+void split_args(cwgpu_context* ctx, const int32_t* d_pairs, const int32_t* d_order, int64_t npairs, int64_t nlong,
+                float* d_dist, cwgpu_pair_stats* d_stats, cwgpu::PairArgs* gl, cwgpu::PairArgs* gs) {
+    *gl = make_args(ctx, d_pairs, d_order, nlong, d_dist, d_stats);
+    *gs = make_args(ctx, d_pairs, d_order + nlong, npairs - nlong, d_dist, d_stats);
+    gs->counter = ctx->d_counter + 4;
+    if (nlong > 0) gs->scratch += (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1);
 }
 
 int check_kernel_error(cwgpu_context* ctx) {
@@ -369,6 +419,7 @@ int cwgpu_create(int device, cwgpu_context** out) {
     ctx->device = device;
     cudaError_t e = cudaSetDevice(device);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&ctx->prio_low, &ctx->prio_high);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, kCounterWords * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long));
@@ -397,6 +448,14 @@ void cwgpu_destroy(cwgpu_context* ctx) {
     dfree(ctx->d_scratch);
     dfree(ctx->d_counter);
     dfree(ctx->d_err);
+    dfree(ctx->d_pairs1);
+    dfree(ctx->d_order1);
+    dfree(ctx->d_dist1);
+    dfree(ctx->d_stats1);
+    if (ctx->stream_short) cudaStreamSynchronize(ctx->stream_short);
+    if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
+    if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
+    if (ctx->stream_short) cudaStreamDestroy(ctx->stream_short);
     cwgpu_fast_release(ctx);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -464,13 +523,19 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     for (int s = 0; s < nseqs; ++s)
         for (int i = 0; i < lens[s]; ++i) dense[doffs[s] + i] = (int8_t)dense_of[codes[offsets[s] + i]];
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
-    dfree(ctx->d_codes);
-    dfree(ctx->d_offs);
-    dfree(ctx->d_lens);
     ctx->has_seqs = false;
-    CW_CUDA(ctx, cudaMalloc(&ctx->d_codes, packed.size()));
-    CW_CUDA(ctx, cudaMalloc(&ctx->d_offs, sizeof(int64_t) * std::max(1, nseqs)));
-    CW_CUDA(ctx, cudaMalloc(&ctx->d_lens, sizeof(int32_t) * std::max(1, nseqs)));
+    CW_CUDA(ctx, grow(ctx->d_codes, ctx->cap_codes, (int64_t)packed.size()));
+    if (nseqs > ctx->cap_seqs || !ctx->d_offs || !ctx->d_lens || !ctx->d_nres) {
+        int64_t c1 = 0, c2 = 0, c3 = 0;
+        dfree(ctx->d_offs);
+        dfree(ctx->d_lens);
+        dfree(ctx->d_nres);
+        ctx->cap_seqs = 0;
+        CW_CUDA(ctx, grow(ctx->d_offs, c1, nseqs));
+        CW_CUDA(ctx, grow(ctx->d_lens, c2, nseqs));
+        CW_CUDA(ctx, grow(ctx->d_nres, c3, nseqs));
+        ctx->cap_seqs = c1;
+    }
     CW_CUDA(ctx, cudaMemcpy(ctx->d_codes, dense.data(), dense.size(), cudaMemcpyHostToDevice));
     if (nseqs) {
         CW_CUDA(ctx, cudaMemcpy(ctx->d_offs, doffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
@@ -514,41 +579,17 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
         if (e == cudaSuccess) e = cudaMemcpy(p->d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice);
     }
     if (e == cudaSuccess) {
-        // Capture: reset the queue counters, then one persistent launch per
-        // kernel. With both kinds of pairs the short-pair kernel runs beside
-        // the long-pair one at lower priority, so its CTAs take the SM slots
-        // that long-pair CTAs leave as the long queue drains.
-        const int64_t nshort = npairs - p->nlong;
-        cwgpu::PairArgs gl = make_args(ctx, p->d_pairs, p->d_order, p->nlong, p->d_dist, p->d_stats);
-        cwgpu::PairArgs gs = make_args(ctx, p->d_pairs, p->d_order + p->nlong, nshort, p->d_dist, p->d_stats);
-        gs.counter = ctx->d_counter + 4;
-        if (p->nlong > 0) gs.scratch += (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1);
-        const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
-        const bool both = p->nlong > 0 && nshort > 0;
-        int prio_low = 0, prio_high = 0;
-        e = cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
-        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
+        // Capture: reset the queue counters, then one persistent launch per kernel.
+        cwgpu::PairArgs gl, gs;
+        split_args(ctx, p->d_pairs, p->d_order, npairs, p->nlong, p->d_dist, p->d_stats, &gl, &gs);
+        const bool both = gl.npairs > 0 && gs.npairs > 0;
+        e = cudaStreamCreateWithFlags(&p->graph_stream, cudaStreamNonBlocking);
         if (e == cudaSuccess && both) e = cudaStreamCreateWithFlags(&p->fork_stream, cudaStreamNonBlocking);
         if (e == cudaSuccess && both) e = cudaEventCreateWithFlags(&p->fork, cudaEventDisableTiming);
         if (e == cudaSuccess && both) e = cudaEventCreateWithFlags(&p->join, cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaStreamBeginCapture(p->graph_stream, cudaStreamCaptureModeThreadLocal);
         if (e == cudaSuccess) {
-            cudaError_t ce = cudaMemsetAsync(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long),
-                                             p->graph_stream);
-            cudaStream_t short_stream = p->graph_stream;
-            if (ce == cudaSuccess && both) {
-                ce = cudaEventRecord(p->fork, p->graph_stream);
-                if (ce == cudaSuccess) ce = cudaStreamWaitEvent(p->fork_stream, p->fork, 0);
-                short_stream = p->fork_stream;
-            }
-            if (ce == cudaSuccess && p->nlong > 0)
-                ce = launch_persistent<cwgpu::kR>(gl, ctx->grid, smem, prio_high, p->graph_stream);
-            if (ce == cudaSuccess && nshort > 0)
-                ce = launch_persistent<cwgpu::kRShort>(gs, ctx->grid_short, smem, prio_low, short_stream);
-            if (ce == cudaSuccess && both) {
-                ce = cudaEventRecord(p->join, p->fork_stream);
-                if (ce == cudaSuccess) ce = cudaStreamWaitEvent(p->graph_stream, p->join, 0);
-            }
+            const cudaError_t ce = enqueue_pairs(ctx, gl, gs, p->graph_stream, p->fork_stream, p->fork, p->join);
             e = cudaStreamEndCapture(p->graph_stream, &p->graph);
             if (e == cudaSuccess) e = ce;
         }
@@ -623,16 +664,46 @@ void cwgpu_plan_destroy(cwgpu_plan* p) {
     delete p;
 }
 
+// One-shot form: the same launches as a plan, enqueued directly (no graph to
+// build for a single run) on the context's streams and grow-only arrays.
 int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,
                       cwgpu_pair_stats* stats_out) {
     if (!ctx || (npairs > 0 && !dist_out)) return CWGPU_ERR_ARG;
-    cwgpu_plan* p = nullptr;
-    int rc = cwgpu_plan_create(ctx, pairs, npairs, &p);
+    int rc = check_ready(ctx);
     if (rc) return rc;
-    rc = cwgpu_plan_launch(p, nullptr);
-    if (!rc) rc = cwgpu_plan_results(p, dist_out, stats_out);
-    cwgpu_plan_destroy(p);
-    return rc;
+    rc = validate_pairs(ctx, pairs, npairs);
+    if (rc) return rc;
+    if (npairs == 0) return CWGPU_OK;
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    if (npairs > ctx->cap_pairs1) {
+        int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
+        ctx->cap_pairs1 = 0;
+        CW_CUDA(ctx, grow(ctx->d_pairs1, c1, 2 * npairs));
+        CW_CUDA(ctx, grow(ctx->d_order1, c2, npairs));
+        CW_CUDA(ctx, grow(ctx->d_dist1, c3, npairs));
+        CW_CUDA(ctx, grow(ctx->d_stats1, c4, npairs));
+        ctx->cap_pairs1 = npairs;
+    }
+    if (!ctx->stream_short) {
+        CW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream_short, cudaStreamNonBlocking));
+        CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+        CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    }
+    int64_t nlong = 0;
+    const std::vector<int32_t> order = work_order(ctx, pairs, npairs, &nlong);
+    cudaStream_t s = ctx->stream;
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs1, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice, s));
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_order1, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, s));
+    cwgpu::PairArgs gl, gs;
+    split_args(ctx, ctx->d_pairs1, ctx->d_order1, npairs, nlong, ctx->d_dist1, stats_out ? ctx->d_stats1 : nullptr,
+               &gl, &gs);
+    CW_CUDA(ctx, enqueue_pairs(ctx, gl, gs, s, ctx->stream_short, ctx->ev_fork, ctx->ev_join));
+    CW_CUDA(ctx, cudaMemcpyAsync(dist_out, ctx->d_dist1, sizeof(float) * npairs, cudaMemcpyDeviceToHost, s));
+    if (stats_out)
+        CW_CUDA(ctx, cudaMemcpyAsync(stats_out, ctx->d_stats1, sizeof(cwgpu_pair_stats) * npairs,
+                                     cudaMemcpyDeviceToHost, s));
+    CW_CUDA(ctx, cudaStreamSynchronize(s));
+    return check_kernel_error(ctx);
 }
 
 int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,

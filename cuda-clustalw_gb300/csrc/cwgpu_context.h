@@ -49,6 +49,18 @@ struct cwgpu_context {
     unsigned generation = 0;  // bumped whenever device inputs or scratch move
     std::string last_error;
     cwgpu_fast_state* fast = nullptr;  // quick-distance tables (cwgpu_fast.cu), built on first use
+    // Grow-only device arrays of the inputs (capacities in elements).
+    int64_t cap_codes = 0, cap_seqs = 0, cap_go = 0;
+    // One-shot cwgpu_align_pairs: grow-only pair arrays and the second stream
+    // the short-pair kernel runs on beside the long-pair one.
+    int32_t* d_pairs1 = nullptr;
+    int32_t* d_order1 = nullptr;
+    float* d_dist1 = nullptr;
+    cwgpu_pair_stats* d_stats1 = nullptr;
+    int64_t cap_pairs1 = 0;
+    cudaStream_t stream_short = nullptr;
+    int prio_low = 0, prio_high = 0;  // stream priority range of the device
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
 };
 
 #endif  // CWGPU_CONTEXT_H

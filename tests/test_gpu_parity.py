@@ -144,3 +144,23 @@ def test_plan_kernel_count(ctx, name, kernels):
     plan = ctx.plan(range_pairs(len(g["seqs"]), *g["range"]))
     assert plan.kernel_count() == kernels
     plan.close()
+
+
+def test_one_shot_calls_reuse_buffers(ctx, oracle_mod):
+    """cwgpu_align_pairs keeps grow-only device arrays in the context: calls of
+    growing and shrinking sizes, with and without stats, and a re-upload of
+    other sequences in between, all give the oracle's results."""
+    g = load_golden("synth_uneven_40")
+    setup(ctx, g)
+    pairs = range_pairs(40, 0, 40, 0, 40)
+    want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    for sl in (slice(0, 50), slice(0, len(pairs)), slice(100, 130), slice(0, 1)):
+        d = ctx.align_pairs(pairs[sl])
+        assert np.array_equal(d, want["dist"][sl])
+        d, st = ctx.align_pairs(pairs[sl], stats=True)
+        assert np.array_equal(d, want["dist"][sl]) and np.array_equal(st["mm_score"], want["mm_score"][sl])
+    h = load_golden("synth_protein_60x97")
+    setup(ctx, h)
+    p2 = range_pairs(60, 0, 60, 0, 60)
+    d = ctx.align_pairs(p2)
+    assert np.array_equal(d, oracle_mod.align_pairs(h["seqs"], h["matrix"], h["params"], p2)["dist"])
