@@ -14,11 +14,15 @@
 //
 // GB300 form: one warp per pair (a CTA of 32 threads), pairs taken longest
 // first from an atomic queue. The lanes count hits with shared-memory
-// atomics over per-sequence k-tuple position lists (built once per sequence
-// set by k_fast_prep), select the top diagonals in parallel, and enumerate
-// the flagged matches of each k-tuple in the reference's order; lane 0 alone
-// runs the fragment chaining, which is a sequential walk of a linked list, on
-// a shared-memory fragment table with 16-bit fields.
+// atomics (16-bit counts, two per word) over per-sequence k-tuple position
+// lists (built once per sequence set by k_fast_prep), select the top
+// diagonals in parallel, and enumerate the flagged matches of each k-tuple in
+// the reference's order. The fragment list is walked and updated by the whole
+// warp: its top 32 entries in registers, the next ones as records in shared
+// memory, the low-score tail in a per-warp global array. The chain is a
+// dependent sequence of short steps, so throughput comes from pairs in
+// flight: about 13 KB of shared memory per pair at 1,500 residues lets
+// 16 pairs share an SM.
 //
 // Selection: the reference sorts the diagonal counts of positions
 // 1..tl1-1 ascending with its own quicksort and flags around the diagonals that
@@ -122,26 +126,30 @@ struct Args {
     unsigned long long* counter;
     Params P;
     int lmax;  // longest sequence of the set (sizes the shared regions)
+    uint2* overflow;       // per warp: list records below the shared ones
+    long long ovf_stride;  // records per warp (2 * max_aln + 2)
 };
 
 // Shared memory of one pair (one CTA), sizes from lmax:
-//   U       union: counts int32[T] + diag int32[T] (count/select), then the
-//           fragments: v1 | v2 << 16 (uint32[FR]), score int16[FR] and the
-//           score-sorted list R uint16[FR] (chain)
-//   flag    uint8[T], flagged uint16[NF], last uint16[NF], kc2 int16[lmax+1]
-// with T = 2*lmax + 2 diagonals, FR = 2*max_aln + 2 fragments and NF the most
-// diagonals that can be flagged, signif * (2*window + 1) (at most T); `last`
-// (the newest fragment on each flagged diagonal) is indexed like `flagged`.
+//   U       union: counts uint16[T] and diag uint16[T] (count/select), then the
+//           list records of the chain (uint2: v1 | v2 << 16, score), CAP of
+//           them, the part of the score-sorted list below its top 32
+//   flag    one bit per diagonal (T bits), flagged uint16[NF], last uint32[NF]
+// with T = 2*lmax + 2 diagonals and NF the most diagonals that can be
+// flagged, signif * (2*window + 1) (at most T). `last` holds the newest
+// fragment on each flagged diagonal as v1 | score << 16 (0: none) and is
+// indexed like `flagged`. List records below the CAP that fit shared memory
+// live in a per-warp global overflow array (the list's low-score tail, which
+// the chain rarely visits).
 struct Smem {
-    int* cnt;
-    int* diag;
-    unsigned* vv;     // fragment v1 | v2 << 16
-    int16_t* fsa;     // fragment score
-    uint16_t* R;      // the score-sorted list, tail first
-    uint8_t* flag;
+    unsigned* cntw;   // 16-bit counts, two per word (atomics on the word)
+    uint16_t* cnt;    // the same counts as an array
+    uint16_t* diag;
+    uint2* sl;        // list records in shared memory
+    int cap;          // their capacity (a multiple of 32)
+    unsigned* flagw;
     uint16_t* flagged;
-    uint16_t* last;
-    int16_t* kc2;
+    unsigned* last;
 };
 
 __host__ __device__ inline size_t max_flagged(int lmax, int signif, int window) {
@@ -149,43 +157,48 @@ __host__ __device__ inline size_t max_flagged(int lmax, int signif, int window) 
     return nf < T ? nf : T;
 }
 
-__host__ __device__ inline size_t smem_bytes(int lmax, int max_aln, size_t NF, size_t* offs_out = nullptr) {
-    const size_t T = 2 * (size_t)lmax + 2, FR = 2 * (size_t)max_aln + 2;
-    size_t u = 8 * T > 8 * FR ? 8 * T : 8 * FR;
-    u = (u + 15) & ~(size_t)15;
+constexpr int kMinListCap = 256;  // list records in shared memory, at least
+
+// Layout of Smem; returns the bytes. offs_out: flagw, flagged, last.
+__host__ __device__ inline size_t smem_bytes(int lmax, size_t NF, size_t* offs_out = nullptr, int* cap_out = nullptr) {
+    const size_t T = 2 * (size_t)lmax + 2;
+    const size_t Tp = (T + 2 + 1) & ~(size_t)1;  // even: whole words of counts
+    size_t u = 4 * Tp;                            // cnt + diag
+    if (u < 8 * (size_t)kMinListCap) u = 8 * (size_t)kMinListCap;
+    u = (u + 255) & ~(size_t)255;  // 32 records of 8 bytes
     size_t off = u;
-    size_t o_flag = off;
-    off += (T + 15) & ~(size_t)15;
-    size_t o_flagged = off;
+    const size_t o_flag = off;
+    off += ((T + 2 + 31) / 32) * 4;
+    off = (off + 15) & ~(size_t)15;
+    const size_t o_flagged = off;
     off += (2 * NF + 15) & ~(size_t)15;
-    size_t o_last = off;
-    off += (2 * NF + 15) & ~(size_t)15;
-    size_t o_kc2 = off;
-    off += (2 * ((size_t)lmax + 1) + 15) & ~(size_t)15;
+    const size_t o_last = off;
+    off += (4 * NF + 15) & ~(size_t)15;
     if (offs_out) {
         offs_out[0] = o_flag;
         offs_out[1] = o_flagged;
         offs_out[2] = o_last;
-        offs_out[3] = o_kc2;
     }
+    if (cap_out) *cap_out = (int)(u / 8);
     return off;
 }
 
-__device__ Smem carve(int lmax, int max_aln, size_t NF) {
+__device__ Smem carve(int lmax, size_t NF) {
     extern __shared__ __align__(16) unsigned char smem[];
-    size_t o[4];
-    smem_bytes(lmax, max_aln, NF, o);
-    const size_t T = 2 * (size_t)lmax + 2, FR = 2 * (size_t)max_aln + 2;
+    size_t o[3];
+    int cap = 0;
+    smem_bytes(lmax, NF, o, &cap);
+    const size_t T = 2 * (size_t)lmax + 2;
+    const size_t Tp = (T + 2 + 1) & ~(size_t)1;
     Smem S;
-    S.cnt = reinterpret_cast<int*>(smem);
-    S.diag = S.cnt + T;
-    S.vv = reinterpret_cast<unsigned*>(smem);
-    S.fsa = reinterpret_cast<int16_t*>(smem + 4 * FR);
-    S.R = reinterpret_cast<uint16_t*>(smem + 6 * FR);
-    S.flag = smem + o[0];
+    S.cntw = reinterpret_cast<unsigned*>(smem);
+    S.cnt = reinterpret_cast<uint16_t*>(smem);
+    S.diag = S.cnt + Tp;
+    S.sl = reinterpret_cast<uint2*>(smem);
+    S.cap = cap;
+    S.flagw = reinterpret_cast<unsigned*>(smem + o[0]);
     S.flagged = reinterpret_cast<uint16_t*>(smem + o[1]);
-    S.last = reinterpret_cast<uint16_t*>(smem + o[2]);
-    S.kc2 = reinterpret_cast<int16_t*>(smem + o[3]);
+    S.last = reinterpret_cast<unsigned*>(smem + o[2]);
     return S;
 }
 
@@ -206,7 +219,7 @@ __device__ __forceinline__ int warp_sum(int v) {
 // range, so the other sub-ranges cannot change positions want_lo and up.
 // Lane 0 only. The explicit stack holds at most log2(size) + 1 ranges, as the
 // reference's (it always continues with the smaller part).
-__device__ void top_quick_sort(int* a, int* b, int size, int want_lo) {
+__device__ void top_quick_sort(uint16_t* a, uint16_t* b, int size, int want_lo) {
     int lst[50], ust[50], p = 1;
     lst[1] = 1;
     ust[1] = size - 1;
@@ -223,12 +236,12 @@ __device__ void top_quick_sort(int* a, int* b, int size, int want_lo) {
             for (j = j - 1; j > i; j--)
                 if (a[j] <= piv) break;
             if (i < j) {
-                int t = a[i]; a[i] = a[j]; a[j] = t;
+                uint16_t t = a[i]; a[i] = a[j]; a[j] = t;
                 t = b[i]; b[i] = b[j]; b[j] = t;
             }
         }
         j = ust[p];
-        int t = a[i]; a[i] = a[j]; a[j] = t;
+        uint16_t t = a[i]; a[i] = a[j]; a[j] = t;
         t = b[i]; b[i] = b[j]; b[j] = t;
         if (i - lst[p] < ust[p] - i) {
             lst[p + 1] = lst[p];
@@ -251,6 +264,11 @@ __device__ __forceinline__ bool frag_rel_pos(int a1, int b1, int a2, int b2, int
     return a2 + ktup - 1 < a1 && b2 + ktup - 1 < b1;
 }
 
+// Sets the flag bits of diagonals lo..hi.
+__device__ __forceinline__ void set_flags(unsigned* flagw, int lo, int hi) {
+    for (int l = lo; l <= hi; ++l) atomicOr(&flagw[l >> 5], 1u << (l & 31));
+}
+
 // One pair on one warp.
 __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     const Params& P = A.P;
@@ -261,19 +279,23 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     const int tl1 = l1 + l2 - 1;
     const int ktup = P.ktup;
     const int16_t* kc1 = A.kcode + o1;
+    const int16_t* kc2 = A.kcode + o2;  // kc2[p - 1]: code of the k-tuple at 1-based p of seq 2
     const uint16_t* pos2 = A.pos + o2;
     const int32_t* st2 = A.start + (size_t)sj * (P.limit + 2);
 
-    // ---- count hits per diagonal (:198-219)
-    for (int d = lane; d <= tl1 + 1; d += 32) S.cnt[d] = 0;
-    for (int p = lane; p < l2; p += 32) S.kc2[p + 1] = A.kcode[o2 + p];
+    // ---- count hits per diagonal (:198-219), 16-bit counts (at most min(l1, l2))
+    const int ncw = (tl1 + 3) / 2;  // words holding counts 0..tl1+1
+    for (int w = lane; w < ncw; w += 32) S.cntw[w] = 0;
     __syncwarp();
     for (int p1 = 1 + lane; p1 <= l1 - ktup + 1; p1 += 32) {
         const int c = kc1[p1 - 1];
         if (!c) continue;
         const int b = __ldg(st2 + c), e = __ldg(st2 + c + 1);
 #pragma unroll 4
-        for (int k = b; k < e; ++k) atomicAdd(&S.cnt[p1 - __ldg(pos2 + k) + l2], 1);
+        for (int k = b; k < e; ++k) {
+            const int d = p1 - __ldg(pos2 + k) + l2;
+            atomicAdd(&S.cntw[d >> 1], 1u << ((d & 1) << 4));
+        }
     }
     __syncwarp();
 
@@ -308,28 +330,29 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
         else if (eq == kk - gt) mode = 2;    // all diagonals at the boundary fit
         else mode = 3;                       // ties straddle the boundary: the reference's sort decides
     }
-    for (int d = lane; d <= tl1 + 1; d += 32) S.flag[d] = 0;
+    const int nfw = (tl1 + 2 + 31) / 32;
+    for (int w = lane; w < nfw; w += 32) S.flagw[w] = 0;
     __syncwarp();
     if (mode == 3) {
-        for (int d = lane; d <= tl1; d += 32) S.diag[d] = d;
+        for (int d = lane; d <= tl1; d += 32) S.diag[d] = (uint16_t)d;
         __syncwarp();
         if (lane == 0) {
             top_quick_sort(S.cnt, S.diag, tl1, jlo);
             for (int i = tl1 - 1; i >= jlo; --i)
                 if (S.cnt[i] > 0) {
                     const int c = S.diag[i];
-                    for (int l = max(1, c - P.window); l <= min(tl1, c + P.window); ++l) S.flag[l] = 1;
+                    set_flags(S.flagw, max(1, c - P.window), min(tl1, c + P.window));
                 }
         }
     } else if (mode != 0) {
         for (int d = 1 + lane; d <= tl1 - 1; d += 32) {
             const int x = S.cnt[d];
             if (x > 0 && (x > T || (mode == 2 && x == T)))
-                for (int l = max(1, d - P.window); l <= min(tl1, d + P.window); ++l) S.flag[l] = 1;
+                set_flags(S.flagw, max(1, d - P.window), min(tl1, d + P.window));
         }
     }
     if (lane == 0 && tl1 >= 1 && S.cnt[tl1] > 0)  // position tl1 keeps its own diagonal
-        for (int l = max(1, tl1 - P.window); l <= tl1; ++l) S.flag[l] = 1;
+        set_flags(S.flagw, max(1, tl1 - P.window), tl1);
     __syncwarp();
     // Flagged diagonals in ascending order. At most signif centres with
     // 2*window+1 diagonals each can be flagged, which sizes the list (the
@@ -338,7 +361,7 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     int nf = 0;
     for (int base = 1; base <= tl1; base += 32) {
         const int d = base + lane;
-        const bool f = d <= tl1 && S.flag[d];
+        const bool f = d <= tl1 && ((S.flagw[d >> 5] >> (d & 31)) & 1u);
         const unsigned m = __ballot_sync(kFull, f);
         const int at = nf + __popc(m & ((1u << lane) - 1));
         if (f && at < nf_cap) S.flagged[at] = (uint16_t)d;
@@ -351,67 +374,91 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     // ---- chain fragments (:246-398), the whole warp together.
     // The reference keeps every fragment in a list sorted by score (putFrag)
     // and, for each match on a flagged diagonal, walks the list from the best
-    // fragment to the first one the match can follow (the A-loop). Here the
-    // list is the array R[0 .. nfr) of fragment numbers in list order
-    // reversed, R[nfr-1] being the head (maxSoFar): a walk from the head is a
-    // 32-wide scan down from the top of R, and an insertion, which putFrag
-    // makes close to the head, shifts only the entries above it.
-    int nfr = 0, currFrag = 0;
+    // fragment to the first one the match can follow (the A-loop). Here list
+    // entries are records (v1 | v2 << 16, score); the index of the entry at
+    // distance d from the head (maxSoFar) is nfr-1-d. The top 32 entries live
+    // in registers, lane d holding distance d (wf = 1, positions wv, score
+    // ws); indices [base, nfr-32) are the shared records sl[0 .. nsl) and
+    // indices below base the warp's global overflow array G. A walk from the
+    // head is a register test and then 32-wide scans down the rest. putFrag
+    // inserts close to the head: within the top 32 it is a register shift
+    // whose last entry joins the shared records; deeper it shifts the records
+    // above it. When the shared records are full, their lower half moves to G.
+    uint2* const G = A.overflow + (size_t)blockIdx.x * (size_t)A.ovf_stride;
+    const int cap = S.cap;
+    int nfr = 0, currFrag = 0, base = 0, nsl = 0;
     bool partial = false;
+    int wf = 0, ws = 0;
+    unsigned wv = 0;
+    const int fl0 = lane < nf ? (int)S.flagged[lane] : 0;
+    const int fl1 = 32 + lane < nf ? (int)S.flagged[32 + lane] : 0;
     for (int i = 1; i <= l1 - ktup + 1 && !partial; ++i) {
         const int c1 = kc1[i - 1];
         if (!c1) continue;
-        for (int base = 0; base < nf && !partial; base += 32) {
-            const int k = base + lane;
-            int vn2 = 0;
+        for (int fb = 0; fb < nf && !partial; fb += 32) {
+            const int k = fb + lane;
+            int fd = 0;
             bool hit = false;
             if (k < nf) {
-                vn2 = i - (int)S.flagged[k] + l2;  // osptr = i - vn2 + l2 = flagged[k]
-                hit = vn2 >= 1 && vn2 <= l2 - ktup + 1 && S.kc2[vn2] == c1;
+                fd = fb == 0 ? fl0 : (fb == 32 ? fl1 : (int)S.flagged[k]);
+                const int vn2 = i - fd + l2;  // osptr = i - vn2 + l2 = flagged[k]
+                hit = vn2 >= 1 && vn2 <= l2 - ktup + 1 && __ldg(kc2 + vn2 - 1) == c1;
             }
             unsigned m = __ballot_sync(kFull, hit);
             // ascending diagonal = descending vn2: the order of the reference's list
             while (m && !partial) {
                 const int t = __ffs(m) - 1;
                 m &= m - 1;
-                const int fi = base + t;  // position of the diagonal in `flagged`
-                const int osptr = S.flagged[fi];
+                const int fi = fb + t;  // position of the diagonal in `flagged`
+                const int osptr = __shfl_sync(kFull, fd, t);
                 const int v2 = i - osptr + l2;
                 // the A-loop: first fragment from the head this match can follow
-                int found = 0;
-                for (int kb = 0; kb < nfr; kb += 32) {
-                    const int kk2 = kb + lane;
-                    int idx = 0;
-                    bool ok = false;
-                    if (kk2 < nfr) {
-                        idx = S.R[nfr - 1 - kk2];
-                        const unsigned vv = S.vv[idx];
-                        ok = frag_rel_pos(i, v2, (int)(vv & 0xffffu), (int)(vv >> 16), ktup);
-                    }
-                    const unsigned mm = __ballot_sync(kFull, ok);
-                    if (mm) {
-                        found = __shfl_sync(kFull, idx, __ffs(mm) - 1);
-                        break;
+                bool found = false;
+                int tfs = 0;
+                unsigned fvv = 0;
+                unsigned mm = __ballot_sync(kFull, wf != 0 && frag_rel_pos(i, v2, (int)(wv & 0xffffu), (int)(wv >> 16), ktup));
+                if (mm) {
+                    const int src = __ffs(mm) - 1;
+                    found = true;
+                    fvv = __shfl_sync(kFull, wv, src);
+                    tfs = __shfl_sync(kFull, ws, src);
+                } else {
+                    for (int kb = 32; kb < nfr; kb += 32) {
+                        const int d = kb + lane;
+                        uint2 r = make_uint2(0u, 0u);
+                        bool ok = false;
+                        if (d < nfr) {
+                            const int j = nfr - 1 - d;
+                            r = j >= base ? S.sl[j - base] : G[j];
+                            ok = frag_rel_pos(i, v2, (int)(r.x & 0xffffu), (int)(r.x >> 16), ktup);
+                        }
+                        mm = __ballot_sync(kFull, ok);
+                        if (mm) {
+                            const int src = __ffs(mm) - 1;
+                            found = true;
+                            fvv = __shfl_sync(kFull, r.x, src);
+                            tfs = (int)__shfl_sync(kFull, r.y, src);
+                            break;
+                        }
                     }
                 }
                 int fs = ktup;
                 if (found) {
-                    const unsigned vv = S.vv[found];
-                    const int tv1 = (int)(vv & 0xffffu), tv2 = (int)(vv >> 16);
-                    const int tfs = S.fsa[found];
+                    const int tv1 = (int)(fvv & 0xffffu), tv2 = (int)(fvv >> 16);
                     if (i - v2 == tv1 - tv2) {
                         fs = tfs + (i > tv1 + (ktup - 1) ? ktup : i - tv1);
                     } else {
-                        const int lf = S.last[fi];
+                        const unsigned lf = S.last[fi];
                         int subt1 = ktup;
                         if (lf) {
-                            const int lv1 = (int)(S.vv[lf] & 0xffffu);
-                            subt1 = S.fsa[lf] + (i > lv1 + (ktup - 1) ? ktup : i - lv1);
+                            const int lv1 = (int)(lf & 0xffffu);
+                            subt1 = (int)(int16_t)(lf >> 16) + (i > lv1 + (ktup - 1) ? ktup : i - lv1);
                         }
                         const int subt2 = tfs - P.window_gap + ktup;
                         fs = subt2 > subt1 ? subt2 : subt1;
                     }
                 }
+                fs = (int16_t)fs;  // the stored score type (never truncates: fs <= ktup * l1 < 2^15)
                 currFrag = nfr + 1;
                 if (currFrag >= 2 * P.max_aln) {
                     partial = true;
@@ -420,39 +467,95 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
                 // putFrag: before the first fragment from the head whose score
                 // is not above fs (the tail if none)
                 int kins = nfr;
-                for (int kb = 0; kb < nfr; kb += 32) {
-                    const int kk2 = kb + lane;
-                    const bool le = kk2 < nfr && S.fsa[S.R[nfr - 1 - kk2]] <= fs;
-                    const unsigned mm = __ballot_sync(kFull, le);
-                    if (mm) {
-                        kins = kb + __ffs(mm) - 1;
-                        break;
+                mm = __ballot_sync(kFull, wf != 0 && ws <= fs);
+                if (mm) {
+                    kins = __ffs(mm) - 1;
+                } else {
+                    for (int kb = 32; kb < nfr; kb += 32) {
+                        const int d = kb + lane;
+                        bool le = false;
+                        if (d < nfr) {
+                            const int j = nfr - 1 - d;
+                            le = (int)(j >= base ? S.sl[j - base].y : G[j].y) <= fs;
+                        }
+                        mm = __ballot_sync(kFull, le);
+                        if (mm) {
+                            kins = kb + __ffs(mm) - 1;
+                            break;
+                        }
                     }
                 }
-                const int pnew = nfr - kins;  // the new fragment's index in R
-                for (int top = nfr - 1; top >= pnew; top -= 32) {  // R[pnew..nfr) up one, top chunk first
-                    const int x = top - lane;
-                    uint16_t v = 0;
-                    if (x >= pnew) v = S.R[x];
+                if (nfr >= 32 && nsl == cap) {  // make room: the lower half of the records to G
+                    const int h = cap / 2;
+                    for (int e = lane; e < h; e += 32) G[base + e] = S.sl[e];
                     __syncwarp();
-                    if (x >= pnew) S.R[x + 1] = v;
+                    for (int e = lane; e < cap - h; e += 32) {
+                        const uint2 v = S.sl[h + e];
+                        S.sl[e] = v;
+                    }
                     __syncwarp();
+                    base += h;
+                    nsl -= h;
                 }
-                if (lane == 0) {
-                    S.vv[currFrag] = (unsigned)i | ((unsigned)v2 << 16);
-                    S.fsa[currFrag] = (int16_t)fs;
-                    S.R[pnew] = (uint16_t)currFrag;
-                    S.last[fi] = (uint16_t)currFrag;
+                const unsigned nv = (unsigned)i | ((unsigned)v2 << 16);
+                if (kins < 32) {
+                    // Into the registers: distance 31 (if any) becomes index nfr - 32.
+                    if (nfr >= 32) {
+                        if (lane == 31) S.sl[nsl] = make_uint2(wv, (unsigned)ws);
+                        ++nsl;
+                    }
+                    const int uf = __shfl_up_sync(kFull, wf, 1);
+                    const unsigned uv = __shfl_up_sync(kFull, wv, 1);
+                    const int us = __shfl_up_sync(kFull, ws, 1);
+                    if (lane > kins) {
+                        wf = uf;
+                        wv = uv;
+                        ws = us;
+                    } else if (lane == kins) {
+                        wf = 1;
+                        wv = nv;
+                        ws = fs;
+                    }
+                } else {
+                    const int pnew = nfr - kins;  // the new record's index (<= nfr - 32)
+                    const uint2 nrec = make_uint2(nv, (unsigned)fs);
+                    const int lo = pnew >= base ? pnew - base : 0;
+                    for (int top = nsl - 1; top >= lo; top -= 32) {  // sl[lo .. nsl) up one, top chunk first
+                        const int x = top - lane;
+                        uint2 v = make_uint2(0u, 0u);
+                        if (x >= lo) v = S.sl[x];
+                        __syncwarp();
+                        if (x >= lo) S.sl[x + 1] = v;
+                        __syncwarp();
+                    }
+                    if (pnew >= base) {
+                        if (lane == 0) S.sl[lo] = nrec;
+                    } else {  // G[base-1] moves up into sl[0]; G[pnew .. base-1) up one
+                        if (lane == 0) S.sl[0] = G[base - 1];
+                        __syncwarp();
+                        for (int top = base - 2; top >= pnew; top -= 32) {
+                            const int x = top - lane;
+                            uint2 v = make_uint2(0u, 0u);
+                            if (x >= pnew) v = G[x];
+                            __syncwarp();
+                            if (x >= pnew) G[x + 1] = v;
+                            __syncwarp();
+                        }
+                        if (lane == 0) G[pnew] = nrec;
+                    }
+                    ++nsl;
                 }
+                if (lane == 0) S.last[fi] = (unsigned)(uint16_t)i | ((unsigned)(uint16_t)fs << 16);
                 __syncwarp();
                 nfr = currFrag;
             }
         }
     }
+    const int head_score = __shfl_sync(kFull, ws, 0);
 
     // ---- distance (:88-103), in double as the reference
     if (lane == 0) {
-        const int score = nfr ? S.fsa[S.R[nfr - 1]] : 0;
+        const int score = nfr ? head_score : 0;
         double calc = 0.0;
         if (nfr) {
             calc = (double)score;
@@ -472,7 +575,7 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
 }
 
 __global__ void __launch_bounds__(32) k_fast(Args A) {
-    const Smem S = carve(A.lmax, A.P.max_aln, max_flagged(A.lmax, A.P.signif, A.P.window));
+    const Smem S = carve(A.lmax, max_flagged(A.lmax, A.P.signif, A.P.window));
     const int lane = threadIdx.x;
     for (;;) {
         unsigned long long k = 0;
@@ -499,12 +602,14 @@ struct cwgpu_fast_state {
     int limit = 0;
     unsigned long long* d_counter = nullptr;
     size_t smem_set = 0;
+    uint2* d_ovf = nullptr;  // list overflow, ovf_records per warp of the grid
+    size_t ovf_bytes = 0;
 };
 
 void cwgpu_fast_release(cwgpu_context* ctx) {
     if (!ctx || !ctx->fast) return;
     cwgpu_fast_state* F = ctx->fast;
-    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter};
+    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter, F->d_ovf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete F;
@@ -595,7 +700,7 @@ int ensure_tables(cwgpu_context* ctx, const Params& P) {
 int run_fast(cwgpu_context* ctx, const Params& P, const int32_t* d_pairs, const int32_t* d_order, long long npairs,
              double* d_dist, cwgpu_fast_stats* d_stats, cudaStream_t st) {
     cwgpu_fast_state* F = ctx->fast;
-    const size_t sm = smem_bytes(ctx->lmax, P.max_aln, max_flagged(ctx->lmax, P.signif, P.window));
+    const size_t sm = smem_bytes(ctx->lmax, max_flagged(ctx->lmax, P.signif, P.window));
     if (sm > 227 * 1024) return ffail(ctx, CWGPU_ERR_ARG, "sequences too long for the quick path's shared memory");
     if (sm > F->smem_set) {
         FAST_CUDA(ctx, cudaFuncSetAttribute(k_fast, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm));
@@ -605,6 +710,15 @@ int run_fast(cwgpu_context* ctx, const Params& P, const int32_t* d_pairs, const 
     FAST_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_fast, 32, sm));
     if (per_sm < 1) return ffail(ctx, CWGPU_ERR_ARG, "quick path does not fit one SM");
     const long long grid = std::min<long long>((long long)per_sm * ctx->sm_count, std::max<long long>(npairs, 1));
+    const long long ovf_records = 2LL * P.max_aln + 2;
+    const size_t ovf = (size_t)grid * (size_t)ovf_records * sizeof(uint2);
+    if (ovf > F->ovf_bytes) {
+        if (F->d_ovf) FAST_CUDA(ctx, cudaFree(F->d_ovf));
+        F->d_ovf = nullptr;
+        F->ovf_bytes = 0;
+        FAST_CUDA(ctx, cudaMalloc(&F->d_ovf, ovf));
+        F->ovf_bytes = ovf;
+    }
     Args A;
     A.kcode = F->d_kcode;
     A.pos = F->d_pos;
@@ -619,6 +733,8 @@ int run_fast(cwgpu_context* ctx, const Params& P, const int32_t* d_pairs, const 
     A.counter = F->d_counter;
     A.P = P;
     A.lmax = ctx->lmax;
+    A.overflow = F->d_ovf;
+    A.ovf_stride = ovf_records;
     FAST_CUDA(ctx, cudaMemsetAsync(F->d_counter, 0, sizeof(unsigned long long), st));
     if (npairs > 0) {
         k_fast<<<(unsigned)grid, 32, sm, st>>>(A);

@@ -113,6 +113,21 @@ def test_gpu_fast_long_family(ctx, oracle_mod):
     assert st["frags"].max() > 1000
 
 
+@pytest.mark.parametrize("ktup,window,signif,partial", [(2, 5, 5, False), (3, 20, 10, False), (2, 20, 10, True)])
+def test_gpu_fast_list_tiers(ctx, oracle_mod, ktup, window, signif, partial):
+    """The fragment list spans its three tiers (registers, shared records,
+    global overflow): DNA families with wide windows give more fragments
+    than fit the shared records (about lmax of them), with deep putFrag
+    insertions among many off-diagonal fragments; the last case fills the
+    list up to the reference's cut-off."""
+    from clustalw_gb300 import synth
+
+    seqs = synth.dna_family(6, 1200, 71)
+    st = check(ctx, oracle_mod, seqs, params(dna=1, ktup=ktup, window=window, window_gap=5, signif=signif, seqs=seqs))
+    assert st["frags"].max() > 1.3 * max(len(s) for s in seqs)
+    assert bool(st["partial"].any()) == partial
+
+
 def test_gpu_fast_device_entry_point(ctx, oracle_mod):
     torch = pytest.importorskip("torch")
     from clustalw_gb300 import native, synth
