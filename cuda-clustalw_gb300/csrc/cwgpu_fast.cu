@@ -604,12 +604,19 @@ struct cwgpu_fast_state {
     size_t smem_set = 0;
     uint2* d_ovf = nullptr;  // list overflow, ovf_records per warp of the grid
     size_t ovf_bytes = 0;
+    // cwgpu_fast_align_pairs: grow-only pair, order and output arrays
+    int32_t* d_pairs = nullptr;
+    int32_t* d_order = nullptr;
+    double* d_dist = nullptr;
+    cwgpu_fast_stats* d_stats = nullptr;
+    int64_t cap_pairs = 0;
 };
 
 void cwgpu_fast_release(cwgpu_context* ctx) {
     if (!ctx || !ctx->fast) return;
     cwgpu_fast_state* F = ctx->fast;
-    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter, F->d_ovf};
+    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter, F->d_ovf,
+                    F->d_pairs, F->d_order, F->d_dist, F->d_stats};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete F;
@@ -762,46 +769,53 @@ int cwgpu_fast_align_pairs(cwgpu_context* ctx, const cwgpu_fast_params* p, const
     if (npairs == 0) return CWGPU_OK;
     rc = ensure_tables(ctx, P);
     if (rc) return rc;
-    // Longest pairs first: the hit count and the chain grow with l1 * l2.
-    std::vector<int32_t> order(npairs);
-    std::iota(order.begin(), order.end(), 0);
-    std::stable_sort(order.begin(), order.end(), [&](int32_t x, int32_t y) {
-        const long long wx = (long long)ctx->lens[pairs[2 * x]] * ctx->lens[pairs[2 * x + 1]];
-        const long long wy = (long long)ctx->lens[pairs[2 * y]] * ctx->lens[pairs[2 * y + 1]];
-        return wx > wy;
-    });
-    int32_t *d_pairs = nullptr, *d_order = nullptr;
-    double* d_dist = nullptr;
-    cwgpu_fast_stats* d_stats = nullptr;
-    cudaStream_t st = ctx->stream;
-    auto cleanup = [&]() {
-        if (d_pairs) cudaFree(d_pairs);
-        if (d_order) cudaFree(d_order);
-        if (d_dist) cudaFree(d_dist);
-        if (d_stats) cudaFree(d_stats);
-    };
-    cudaError_t e = cudaMalloc(&d_pairs, sizeof(int32_t) * 2 * npairs);
-    if (e == cudaSuccess) e = cudaMalloc(&d_order, sizeof(int32_t) * npairs);
-    if (e == cudaSuccess) e = cudaMalloc(&d_dist, sizeof(double) * npairs);
-    if (e == cudaSuccess && stats_out) e = cudaMalloc(&d_stats, sizeof(cwgpu_fast_stats) * npairs);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess)
-        e = cudaMemcpyAsync(d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, st);
-    if (e != cudaSuccess) {
-        cleanup();
-        return ffail(ctx, e == cudaErrorMemoryAllocation ? CWGPU_ERR_OOM : CWGPU_ERR_CUDA,
-                     std::string("quick path set-up: ") + cudaGetErrorString(e));
+    // Longest pairs first: the hit count and the chain grow with l1 * l2. The
+    // order only balances the load: a stable counting sort on the top 12
+    // bits of l1 * l2 as a float.
+    constexpr int kKeyBits = 12, kBuckets = 1 << kKeyBits;
+    std::vector<uint16_t> key((size_t)npairs);
+    std::vector<int64_t> start(kBuckets + 1, 0);
+    for (int64_t q = 0; q < npairs; ++q) {
+        const float w = (float)((double)ctx->lens[pairs[2 * q]] * (double)ctx->lens[pairs[2 * q + 1]]);
+        uint32_t bits;
+        memcpy(&bits, &w, sizeof(bits));
+        const int k = kBuckets - 1 - (int)(bits >> (31 - kKeyBits));
+        key[(size_t)q] = (uint16_t)k;
+        ++start[k + 1];
     }
+    for (int k = 0; k < kBuckets; ++k) start[k + 1] += start[k];
+    std::vector<int32_t> order((size_t)npairs);
+    for (int64_t q = 0; q < npairs; ++q) order[(size_t)start[key[(size_t)q]]++] = (int32_t)q;
+    cwgpu_fast_state* F = ctx->fast;
+    cudaStream_t st = ctx->stream;
+    if (npairs > F->cap_pairs) {
+        void* old[] = {F->d_pairs, F->d_order, F->d_dist, F->d_stats};
+        for (void* ptr : old)
+            if (ptr) cudaFree(ptr);
+        F->d_pairs = F->d_order = nullptr;
+        F->d_dist = nullptr;
+        F->d_stats = nullptr;
+        F->cap_pairs = 0;
+        FAST_CUDA(ctx, cudaMalloc(&F->d_pairs, sizeof(int32_t) * 2 * npairs));
+        FAST_CUDA(ctx, cudaMalloc(&F->d_order, sizeof(int32_t) * npairs));
+        FAST_CUDA(ctx, cudaMalloc(&F->d_dist, sizeof(double) * npairs));
+        FAST_CUDA(ctx, cudaMalloc(&F->d_stats, sizeof(cwgpu_fast_stats) * npairs));
+        F->cap_pairs = npairs;
+    }
+    int32_t* d_pairs = F->d_pairs;
+    int32_t* d_order = F->d_order;
+    double* d_dist = F->d_dist;
+    cwgpu_fast_stats* d_stats = stats_out ? F->d_stats : nullptr;
+    FAST_CUDA(ctx, cudaMemcpyAsync(d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice, st));
+    FAST_CUDA(ctx, cudaMemcpyAsync(d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, st));
     rc = run_fast(ctx, P, d_pairs, d_order, npairs, d_dist, d_stats, st);
     if (rc == CWGPU_OK) {
-        e = cudaMemcpyAsync(dist_out, d_dist, sizeof(double) * npairs, cudaMemcpyDeviceToHost, st);
+        cudaError_t e = cudaMemcpyAsync(dist_out, d_dist, sizeof(double) * npairs, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess && stats_out)
             e = cudaMemcpyAsync(stats_out, d_stats, sizeof(cwgpu_fast_stats) * npairs, cudaMemcpyDeviceToHost, st);
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         if (e != cudaSuccess) rc = ffail(ctx, CWGPU_ERR_CUDA, std::string("quick path: ") + cudaGetErrorString(e));
     }
-    cleanup();
     return rc;
 }
 
