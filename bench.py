@@ -523,13 +523,13 @@ def ours_arm(args):
     ctx.set_matrix(matrix)
     ctx.set_params(params)
     ctx.upload_seqs(packed=packed)
-    tuning = {"tiny_m_tiny_n": list(ctx.get_tuning()), "autotuned": False}
+    tuning = {"tiny_m_tiny_n_short_rows": list(ctx.get_tuning()), "autotuned": False}
     if args.autotune:
         from clustalw_gb300 import autotune
 
         choice, timings = autotune.tune(ctx, packed[2], pairs, gpu_name=torch.cuda.get_device_name(local))
-        tuning = {"tiny_m_tiny_n": list(choice), "autotuned": True,
-                  "candidates_s": {f"{m},{n}": round(t, 4) for (m, n), t in timings.items()}}
+        tuning = {"tiny_m_tiny_n_short_rows": list(choice), "autotuned": True,
+                  "candidates_s": {",".join(map(str, c)): round(t, 4) for c, t in timings.items()}}
     plan = ctx.plan(pairs)
     # A dedicated stream: the graph is launched on it and the CUDA events are
     # recorded on it (torch's default stream has handle 0, which the C ABI

@@ -1,13 +1,16 @@
 """Autotuner for the kernel's tunable knobs (cwgpu_tuning).
 
-The knobs are the bin thresholds of the Myers-Miller stage: frames with at
-most `tiny_m` rows and `tiny_n` columns are solved one frame per lane, the rest
-by warp-wide sweeps. The best split depends on the length distribution of the
-workload (short families produce mostly tiny frames, long ones mostly large),
-so the tuner times a length-stratified sample of the workload's pairs under
-each candidate and keeps the fastest. Results never depend on the knobs, only
-the time does. Choices are cached per GPU and length profile in
-$XDG_CACHE_HOME/clustalw_gb300/tuning.json.
+The knobs are bin thresholds. In the Myers-Miller stage, frames with at most
+`tiny_m` rows and `tiny_n` columns are solved one frame per lane, the rest by
+warp-wide sweeps. Across pairs, those whose first sequence has at most
+`short_rows` residues run in the short-pair kernel (4 rows per lane), the rest
+in the long-pair kernel (8 rows per lane). The best splits depend on the length
+distribution of the workload (short families produce mostly tiny frames, long
+ones mostly large), so the tuner times a length-stratified sample of the
+workload's pairs: first each tiny-frame candidate, then each short-pair
+threshold with the chosen tiny-frame pair, and keeps the fastest. Results never
+depend on the knobs, only the time does. Choices are cached per GPU and length
+profile in $XDG_CACHE_HOME/clustalw_gb300/tuning.json.
 """
 import json
 import os
@@ -16,6 +19,7 @@ import time
 import numpy as np
 
 CANDIDATES = [(0, 0), (16, 8), (16, 16), (32, 12), (32, 16), (64, 16)]
+SHORT_ROWS = [0, 64, 128, 192, 256]
 
 
 def _cache_path():
@@ -49,9 +53,24 @@ def stratified_sample(lens, pairs, target_cells, seed=0):
     return pairs[np.sort(np.concatenate(pick))]
 
 
-def tune(ctx, lens, pairs, gpu_name="gpu", target_cells=2e10, candidates=CANDIDATES, use_cache=True, repeats=2):
-    """Pick (tiny_m, tiny_n) for this workload on `ctx` (a native.Context with
-    matrix, params and sequences set), apply it and return
+def _time_sample(ctx, sample, repeats):
+    plan = ctx.plan(sample)
+    plan.launch()
+    plan.results()
+    best = float("inf")
+    for _ in range(repeats):
+        t = time.perf_counter()
+        plan.launch()
+        plan.results()
+        best = min(best, time.perf_counter() - t)
+    plan.close()
+    return best
+
+
+def tune(ctx, lens, pairs, gpu_name="gpu", target_cells=2e10, candidates=CANDIDATES, short_rows=SHORT_ROWS,
+         use_cache=True, repeats=2):
+    """Pick (tiny_m, tiny_n, short_rows) for this workload on `ctx` (a
+    native.Context with matrix, params and sequences set), apply it and return
     (choice, {candidate: seconds})."""
     key = f"{gpu_name}|{length_profile(lens)}"
     path = _cache_path()
@@ -62,29 +81,34 @@ def tune(ctx, lens, pairs, gpu_name="gpu", target_cells=2e10, candidates=CANDIDA
                 cache = json.load(f)
         except (OSError, ValueError):
             cache = {}
-    if use_cache and key in cache:
+    if use_cache and key in cache and len(cache[key].get("choice", [])) == 3:
         choice = tuple(cache[key]["choice"])
         ctx.set_tuning(*choice)
         return choice, {}
     sample = stratified_sample(lens, pairs, target_cells)
+    lens = np.asarray(lens)
+    first = lens[np.asarray(sample).reshape(-1, 2)[:, 0]] if len(sample) else lens[:0]
+    rows0 = ctx.get_tuning()[2]
     timings = {}
     for cand in candidates:
-        ctx.set_tuning(*cand)
-        plan = ctx.plan(sample)
-        plan.launch()
-        plan.results()
-        best = float("inf")
-        for _ in range(repeats):
-            t = time.perf_counter()
-            plan.launch()
-            plan.results()
-            best = min(best, time.perf_counter() - t)
-        plan.close()
-        timings[cand] = best
+        ctx.set_tuning(cand[0], cand[1], rows0)
+        timings[(cand[0], cand[1], rows0)] = _time_sample(ctx, sample, repeats)
+    tiny = min(timings, key=timings.get)[:2]
+    # A threshold only matters if it splits the sample differently from the others.
+    seen = set()
+    for r in short_rows:
+        split = int((first <= r).sum())
+        if split in seen and r != rows0:
+            continue
+        seen.add(split)
+        cand = (tiny[0], tiny[1], r)
+        if cand not in timings:
+            ctx.set_tuning(*cand)
+            timings[cand] = _time_sample(ctx, sample, repeats)
     choice = min(timings, key=timings.get)
     ctx.set_tuning(*choice)
     if use_cache:
-        cache[key] = {"choice": list(choice), "seconds": {f"{m},{n}": s for (m, n), s in timings.items()}}
+        cache[key] = {"choice": list(choice), "seconds": {",".join(map(str, c)): s for c, s in timings.items()}}
         try:
             os.makedirs(os.path.dirname(path), exist_ok=True)
             with open(path, "w") as f:

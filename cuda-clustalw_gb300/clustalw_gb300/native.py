@@ -96,7 +96,7 @@ FAST_STATS_DTYPE = np.dtype([("score", "<i4"), ("frags", "<i4"), ("partial", "<i
 class Tuning(ctypes.Structure):
     """cwgpu_tuning: tiny-frame thresholds of the Myers-Miller stage."""
 
-    _fields_ = [("tiny_m", ctypes.c_int32), ("tiny_n", ctypes.c_int32)]
+    _fields_ = [("tiny_m", ctypes.c_int32), ("tiny_n", ctypes.c_int32), ("short_rows", ctypes.c_int32)]
 
 
 class ServerOpts(ctypes.Structure):
@@ -341,14 +341,17 @@ class Context:
     def plan(self, pairs):
         return Plan(self, pairs)
 
-    def set_tuning(self, tiny_m, tiny_n):
-        t = Tuning(int(tiny_m), int(tiny_n))
+    def set_tuning(self, tiny_m, tiny_n, short_rows=None):
+        """Sets the knobs of cwgpu_tuning; short_rows None keeps the current value."""
+        if short_rows is None:
+            short_rows = self.get_tuning()[2]
+        t = Tuning(int(tiny_m), int(tiny_n), int(short_rows))
         self._check(self._lib.cwgpu_set_tuning(self._h, ctypes.byref(t)), "cwgpu_set_tuning")
 
     def get_tuning(self):
         t = Tuning()
         self._check(self._lib.cwgpu_get_tuning(self._h, ctypes.byref(t)), "cwgpu_get_tuning")
-        return t.tiny_m, t.tiny_n
+        return t.tiny_m, t.tiny_n, t.short_rows
 
     def synchronize(self):
         self._check(self._lib.cwgpu_synchronize(self._h), "cwgpu_synchronize")

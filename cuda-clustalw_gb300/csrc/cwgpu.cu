@@ -32,8 +32,9 @@ constexpr int kWarpsPerBlock = 4;  // warps (= concurrent pairs) per CTA
 constexpr int kCounterWords = 8;   // cwgpu_context::d_counter
 
 // RS = rows per lane of every sweep: cwgpu::kR for the long-pair kernel,
-// cwgpu::kRShort for pairs whose first sequence has at most kShortRows
-// residues. Separate kernels keep the long-pair code exactly as tuned.
+// cwgpu::kRShort for pairs whose first sequence has at most
+// cwgpu_tuning::short_rows residues (128 by default: one 4-row stripe).
+// Separate kernels keep the long-pair code exactly as tuned.
 template <int RS>
 __global__ void __launch_bounds__(kWarpsPerBlock * 32, RS == cwgpu::kR ? 0 : 5)
     k_pairwise(cwgpu::PairArgs g, long long single) {
@@ -189,7 +190,7 @@ int persistent_grid(cwgpu_context* ctx, int* grid) {
 
 bool has_short_seqs(const cwgpu_context* ctx) {
     for (int s = 0; s < ctx->nseqs; ++s)
-        if (ctx->lens[s] <= cwgpu::kShortRows) return true;
+        if (ctx->lens[s] <= ctx->short_rows) return true;
     return false;
 }
 
@@ -268,7 +269,7 @@ int validate_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs) {
 }
 
 bool short_pair(const cwgpu_context* ctx, const int32_t* pairs, int64_t q) {
-    return ctx->lens[pairs[2 * q]] <= cwgpu::kShortRows;
+    return ctx->lens[pairs[2 * q]] <= ctx->short_rows;
 }
 
 // Pairs for the long-pair kernel first, then those for the short-pair kernel
@@ -779,10 +780,12 @@ int cwgpu_pairwise_align(cwgpu_context* ctx, int32_t i_start, int32_t i_end, int
 
 int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning) {
     if (!ctx || !tuning) return CWGPU_ERR_ARG;
-    if (tuning->tiny_m < 0 || tuning->tiny_m > 256 || tuning->tiny_n < 0 || tuning->tiny_n > cwgpu::kTinyMaxN)
-        return fail(ctx, CWGPU_ERR_ARG, "tiny_m must be in [0, 256] and tiny_n in [0, 16]");
+    if (tuning->tiny_m < 0 || tuning->tiny_m > 256 || tuning->tiny_n < 0 || tuning->tiny_n > cwgpu::kTinyMaxN ||
+        tuning->short_rows < 0 || tuning->short_rows > CWGPU_MAX_SEQ_LEN)
+        return fail(ctx, CWGPU_ERR_ARG, "tiny_m must be in [0, 256], tiny_n in [0, 16], short_rows in [0, 65535]");
     ctx->tiny_m = tuning->tiny_m;
     ctx->tiny_n = tuning->tiny_n;
+    ctx->short_rows = tuning->short_rows;
     ctx->generation++;
     return CWGPU_OK;
 }
@@ -791,6 +794,7 @@ int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning) {
     if (!ctx || !tuning) return CWGPU_ERR_ARG;
     tuning->tiny_m = ctx->tiny_m;
     tuning->tiny_n = ctx->tiny_n;
+    tuning->short_rows = ctx->short_rows;
     return CWGPU_OK;
 }
 

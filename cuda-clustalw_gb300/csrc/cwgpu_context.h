@@ -31,6 +31,7 @@ struct cwgpu_context {
     int dense_of[CWGPU_NUMRES];      // original code -> dense index, -1 if absent
     int code_of[CWGPU_NUMRES];       // dense index -> original code
     int tiny_m = 32, tiny_n = 16;    // Myers-Miller frames solved one per lane
+    int short_rows = 128;            // pairs with a first sequence this short: short-pair kernel
     int8_t* d_codes = nullptr;
     int64_t* d_offs = nullptr;
     int32_t* d_lens = nullptr;

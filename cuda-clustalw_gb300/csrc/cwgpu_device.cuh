@@ -46,7 +46,6 @@ namespace cwgpu {
 constexpr unsigned kFull = 0xffffffffu;
 constexpr int kR = 8;              // rows per lane in every sweep of long pairs
 constexpr int kRShort = 4;         // rows per lane in the short-pair kernel
-constexpr int kShortRows = 32 * kRShort;  // pairs whose first sequence fits one 4-row stripe
 constexpr int kTinyMaxN = 16;      // tiny frames: N <= kTinyMaxN (shared-memory rows)
 constexpr int kTinyStride = kTinyMaxN + 1;
 constexpr int kTinyWords = 4 * kTinyStride * 32;  // HH, DD, RR, SS for 32 lanes
@@ -754,7 +753,7 @@ struct PairArgs {
 // the distance and fills `st`; adds the algorithmic cell counts (the
 // inner-loop iterations the reference executes) to acc[0..2]. RS = rows per
 // lane in every sweep: any RS gives the same results; kRShort needs fewer
-// steps when n <= kShortRows (one stripe, lanes of 4 rows instead of
+// warp steps when n <= 128 (one stripe, lanes of 4 rows instead of
 // half-empty lanes of 8).
 template <int RS = kR>
 static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int m, int len1, int len2, int go, int ge,

@@ -194,10 +194,14 @@ int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d_offsets, c
 /* Tuning knobs of the kernel (no reference counterpart; results do not depend
  * on them). Myers-Miller frames with M <= tiny_m rows and N <= tiny_n columns
  * (tiny_n <= 16, tiny_m <= 256) are solved one frame per lane instead of by a
- * warp-wide sweep. The autotuner in clustalw_gb300/autotune.py picks them. */
+ * warp-wide sweep. Pairs whose first sequence has at most short_rows residues
+ * (0..65535; default 128, 0 = none) run in the short-pair kernel (4 rows per
+ * lane) instead of the long-pair one (8 rows per lane). The autotuner in
+ * clustalw_gb300/autotune.py picks all three. */
 typedef struct cwgpu_tuning {
     int32_t tiny_m;
     int32_t tiny_n;
+    int32_t short_rows;
 } cwgpu_tuning;
 int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning);
 int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning);

@@ -164,3 +164,43 @@ def test_one_shot_calls_reuse_buffers(ctx, oracle_mod):
     p2 = range_pairs(60, 0, 60, 0, 60)
     d = ctx.align_pairs(p2)
     assert np.array_equal(d, oracle_mod.align_pairs(h["seqs"], h["matrix"], h["params"], p2)["dist"])
+
+
+@pytest.mark.parametrize("short_rows", [0, 64, 300, 65535])
+def test_short_rows_knob_keeps_results(ctx, oracle_mod, short_rows):
+    """The short-pair threshold moves pairs between the 4-row and 8-row
+    kernels (0: none short, 65535: all short); results stay the oracle's."""
+    g = load_golden("synth_uneven_40")
+    setup(ctx, g)
+    pairs = range_pairs(40, 0, 40, 0, 40)
+    old = ctx.get_tuning()
+    ctx.set_tuning(old[0], old[1], short_rows)
+    try:
+        d, st = ctx.align_pairs(pairs, stats=True)
+        plan = ctx.plan(pairs)
+        kernels = plan.kernel_count()
+        plan.launch()
+        d2 = plan.results()
+        plan.close()
+    finally:
+        ctx.set_tuning(*old)
+    want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    assert np.array_equal(d, want["dist"]) and np.array_equal(d2, want["dist"])
+    for f in STAT_FIELDS:
+        assert np.array_equal(st[f], want[f]), f
+    assert kernels == (1 if short_rows in (0, 65535) else 2)
+
+
+def test_autotune_picks_all_knobs(ctx):
+    from clustalw_gb300 import autotune
+
+    g = load_golden("synth_uneven_40")
+    setup(ctx, g)
+    pairs = range_pairs(40, 0, 40, 0, 40)
+    lens = [len(s) for s in g["seqs"]]
+    before = ctx.align_pairs(pairs)
+    choice, timings = autotune.tune(ctx, lens, pairs, target_cells=2e8, use_cache=False, repeats=1)
+    assert len(choice) == 3 and ctx.get_tuning() == tuple(choice)
+    assert len({c[2] for c in timings}) >= 2  # short-pair thresholds were timed
+    assert np.array_equal(ctx.align_pairs(pairs), before)
+    ctx.set_tuning(32, 16, 128)
