@@ -59,6 +59,7 @@ struct Args {
     double* r;  // sumCols + sumRows of the valid nodes, for the search
     unsigned char* valid;
     int* rep;  // cycle that last formed the cluster node i stands for (0: leaf)
+    int* vlist;  // the valid nodes in ascending order (n + 1 entries)
     unsigned long long* cand_k;  // order key of the criterion
     long long* cand_idx;
     int2* cand_ij;
@@ -287,6 +288,11 @@ struct RowTerms {  // d(i, j) for i < j: row j of the packed triangle
     const double* row;
     __device__ double operator()(int i) const { return __ldcg(row + (i - 1)); }
 };
+struct ListTerms {  // x[list[k]]: the terms of the valid nodes only, in ascending node order
+    const double* x;
+    const int* list;
+    __device__ double operator()(int k) const { return x[list[k]]; }
+};
 struct ColTerms {  // d(j, i) for i > j: column j of the packed triangle
     const double* d;
     int j;
@@ -303,14 +309,14 @@ struct Smem {
     long long* red_i;
     int2* red_ij;
     double* red_d;
-    double* ext;  // sumCols, sumRows, av, join (n+1 each), then rep (n+1 ints)
+    double* ext;  // sumCols, sumRows, av, join (n+1 each), then rep and vlist (n+1 ints each)
 };
 
 __host__ __device__ inline size_t smem_layout(int n, bool node_shared, size_t* ext_off, size_t* v_off) {
     size_t off = sizeof(double) * (size_t)(n + 1);                          // r
     off += (2 * sizeof(double) + sizeof(long long) + sizeof(int2)) * kWarps;  // reduction scratch
     *ext_off = off;
-    if (node_shared) off += 4 * sizeof(double) * (size_t)(n + 1) + sizeof(int) * (size_t)(n + 1);
+    if (node_shared) off += 4 * sizeof(double) * (size_t)(n + 1) + 2 * sizeof(int) * (size_t)(n + 1);
     *v_off = off;
     return off + (size_t)(n + 1) + 16;
 }
@@ -344,6 +350,7 @@ struct Node {
     double* r;
     unsigned char* valid;
     int* rep;
+    int* vlist;  // valid nodes, ascending: the terms of the sequential sums
 };
 
 // A search candidate: criterion, element index (scan order), (ii, jj) and
@@ -605,6 +612,38 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
         if (shared) A.valid[minj] = 0;
     }
     __syncthreads();
+    // minj leaves the list of valid nodes (nv of them before this join: one
+    // node leaves per cycle). The reference's sums run over the valid nodes in
+    // ascending order, skipping the others, which add +0.0 and change nothing,
+    // so the sums below walk the list instead of all n nodes.
+    const int nv = n - nc + 1;
+    __shared__ int s_pi, s_pj, s_bad;
+    if (threadIdx.x == 0) {
+        int lo = 0, hi = nv;  // first k with vlist[k] >= mini, then minj
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (N.vlist[mid] < mini) lo = mid + 1; else hi = mid;
+        }
+        s_pi = lo;
+        hi = nv;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (N.vlist[mid] < minj) lo = mid + 1; else hi = mid;
+        }
+        s_pj = lo;
+        s_bad = !(s_pi < nv && N.vlist[s_pi] == mini && lo < nv && N.vlist[lo] == minj);
+        if (s_bad) atomicCAS(A.status, ST_OK, ST_INTERNAL);
+    }
+    __syncthreads();
+    if (s_bad) return false;
+    const int pi = s_pi;
+    for (int b0 = s_pj; b0 < nv - 1; b0 += blockDim.x) {  // vlist[pj+1 .. nv) down one
+        const int k = b0 + (int)threadIdx.x;
+        const int v = k < nv - 1 ? N.vlist[k + 1] : 0;
+        __syncthreads();
+        if (k < nv - 1) N.vlist[k] = v;
+        __syncthreads();
+    }
     // The reference's three sequential sums on three warps (three SM
     // sub-partitions): sumRows[mini] and sumCols[mini] over the joined row
     // (NJTree.cpp:590-616) and the next cycle's sumd over sumCols
@@ -612,20 +651,20 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
     // The other warps meanwhile form the next search's diq/djq terms.
     double sumd_part = 0.0;
     if (warp == 0) {
-        const double v = warp_seq_sum(ValidTerms{N.join, N.valid}, 1, mini, 0.0);
+        const double v = warp_seq_sum(ListTerms{N.join, N.vlist}, 0, pi, 0.0);
         if (lane == 0) s_sR = v;
     } else if (warp == 1) {
-        const double v = warp_seq_sum(ValidTerms{N.join, N.valid}, mini + 1, n + 1, 0.0);
+        const double v = warp_seq_sum(ListTerms{N.join, N.vlist}, pi + 1, nv - 1, 0.0);
         if (lane == 0) s_sC = v;
     } else if (warp == 2) {
-        sumd_part = warp_seq_sum(ValidTerms{N.sumCols, N.valid}, 1, mini, 0.0);
+        sumd_part = warp_seq_sum(ListTerms{N.sumCols, N.vlist}, 0, pi, 0.0);
     } else {
         publish_r(A, N, shared, 96, mini);
     }
     __syncthreads();
     if (warp == 2) {
         double v = __dadd_rn(sumd_part, s_sC);
-        v = warp_seq_sum(ValidTerms{N.sumCols, N.valid}, mini + 1, n + 1, v);
+        v = warp_seq_sum(ListTerms{N.sumCols, N.vlist}, pi + 1, nv - 1, v);
         if (lane == 0) s_sumd = v;
     }
     __syncthreads();
@@ -732,6 +771,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nj(Args A) {
         N.av = S.ext + 2 * (size_t)(n + 1);
         N.join = S.ext + 3 * (size_t)(n + 1);
         N.rep = reinterpret_cast<int*>(S.ext + 4 * (size_t)(n + 1));
+        N.vlist = N.rep + (n + 1);
         N.r = S.r;
         N.valid = S.v;
         for (int j = threadIdx.x; j <= n; j += blockDim.x) {
@@ -743,8 +783,9 @@ __global__ void __launch_bounds__(kThreads, 1) k_nj(Args A) {
             N.valid[j] = j > 0;
         }
     } else {
-        N = Node{A.sumCols, A.sumRows, A.av, A.join, A.r, A.valid, A.rep};
+        N = Node{A.sumCols, A.sumRows, A.av, A.join, A.r, A.valid, A.rep, A.vlist};
     }
+    for (int k = threadIdx.x; k < n; k += blockDim.x) N.vlist[k] = k + 1;  // every node starts valid
     __syncthreads();
     {
         __shared__ double s_sumd0;
@@ -859,7 +900,7 @@ int ensure(cwgpu_nj* h, int n) {
         NJ_CHECK(h, cudaMalloc(&h->d_joins, (size_t)2 * (n + 1) * sizeof(int)));
         NJ_CHECK(h, cudaMalloc(&h->d_vec, 5 * (size_t)(n + 1) * sizeof(double)));
         NJ_CHECK(h, cudaMalloc(&h->d_valid, (size_t)(n + 1)));
-        NJ_CHECK(h, cudaMalloc(&h->d_rep, (size_t)(n + 1) * sizeof(int)));
+        NJ_CHECK(h, cudaMalloc(&h->d_rep, 2 * (size_t)(n + 1) * sizeof(int)));  // rep, then the valid list
         h->cap_n = n;
     }
     const size_t sm = smem_bytes(n, node_shared_for(h, n));
@@ -915,6 +956,7 @@ int run(cwgpu_nj* h, int n, cudaStream_t st, double* d_left, double* d_right, in
     A.r = h->d_vec + 4 * (size_t)(n + 1);
     A.valid = h->d_valid;
     A.rep = h->d_rep;
+    A.vlist = h->d_rep + (n + 1);
     A.cand_k = h->d_cand_k;
     A.cand_idx = h->d_cand_idx;
     A.cand_ij = h->d_cand_ij;
