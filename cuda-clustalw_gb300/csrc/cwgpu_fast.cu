@@ -21,8 +21,8 @@
 // warp: its top 32 entries in registers, the next ones as records in shared
 // memory, the low-score tail in a per-warp global array. The chain is a
 // dependent sequence of short steps, so throughput comes from pairs in
-// flight: about 13 KB of shared memory per pair at 1,500 residues lets
-// 16 pairs share an SM.
+// flight: about 7 KB of shared memory per pair at 1,500 residues lets 28
+// pairs share an SM.
 //
 // Selection: the reference sorts the diagonal counts of positions
 // 1..tl1-1 ascending with its own quicksort and flags around the diagonals that
@@ -128,23 +128,25 @@ struct Args {
     int lmax;  // longest sequence of the set (sizes the shared regions)
     uint2* overflow;       // per warp: list records below the shared ones
     long long ovf_stride;  // records per warp (2 * max_aln + 2)
+    uint16_t* sortbuf;     // per warp: counts and diagonals for the reference's sort
+    long long sort_stride; // entries per array (2 * lmax + 4)
 };
 
 // Shared memory of one pair (one CTA), sizes from lmax:
-//   U       union: counts uint16[T] and diag uint16[T] (count/select), then the
-//           list records of the chain (uint2: v1 | v2 << 16, score), CAP of
-//           them, the part of the score-sorted list below its top 32
+//   U       union: counts uint16[T] (count/select), then the list records of
+//           the chain (uint2: v1 | v2 << 16, score), CAP of them, the part of
+//           the score-sorted list below its top 32
 //   flag    one bit per diagonal (T bits), flagged uint16[NF], last uint32[NF]
 // with T = 2*lmax + 2 diagonals and NF the most diagonals that can be
 // flagged, signif * (2*window + 1) (at most T). `last` holds the newest
 // fragment on each flagged diagonal as v1 | score << 16 (0: none) and is
 // indexed like `flagged`. List records below the CAP that fit shared memory
 // live in a per-warp global overflow array (the list's low-score tail, which
-// the chain rarely visits).
+// the chain rarely visits). The reference's sort of the counts, needed for
+// about one pair in ten, runs on a per-warp global copy (counts, diagonals).
 struct Smem {
     unsigned* cntw;   // 16-bit counts, two per word (atomics on the word)
     uint16_t* cnt;    // the same counts as an array
-    uint16_t* diag;
     uint2* sl;        // list records in shared memory
     int cap;          // their capacity (a multiple of 32)
     unsigned* flagw;
@@ -163,7 +165,7 @@ constexpr int kMinListCap = 256;  // list records in shared memory, at least
 __host__ __device__ inline size_t smem_bytes(int lmax, size_t NF, size_t* offs_out = nullptr, int* cap_out = nullptr) {
     const size_t T = 2 * (size_t)lmax + 2;
     const size_t Tp = (T + 2 + 1) & ~(size_t)1;  // even: whole words of counts
-    size_t u = 4 * Tp;                            // cnt + diag
+    size_t u = 2 * Tp;                            // cnt
     if (u < 8 * (size_t)kMinListCap) u = 8 * (size_t)kMinListCap;
     u = (u + 255) & ~(size_t)255;  // 32 records of 8 bytes
     size_t off = u;
@@ -188,12 +190,9 @@ __device__ Smem carve(int lmax, size_t NF) {
     size_t o[3];
     int cap = 0;
     smem_bytes(lmax, NF, o, &cap);
-    const size_t T = 2 * (size_t)lmax + 2;
-    const size_t Tp = (T + 2 + 1) & ~(size_t)1;
     Smem S;
     S.cntw = reinterpret_cast<unsigned*>(smem);
     S.cnt = reinterpret_cast<uint16_t*>(smem);
-    S.diag = S.cnt + Tp;
     S.sl = reinterpret_cast<uint2*>(smem);
     S.cap = cap;
     S.flagw = reinterpret_cast<unsigned*>(smem + o[0]);
@@ -334,13 +333,18 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     for (int w = lane; w < nfw; w += 32) S.flagw[w] = 0;
     __syncwarp();
     if (mode == 3) {
-        for (int d = lane; d <= tl1; d += 32) S.diag[d] = (uint16_t)d;
+        uint16_t* const ga = A.sortbuf + (size_t)blockIdx.x * 2 * (size_t)A.sort_stride;
+        uint16_t* const gd = ga + A.sort_stride;
+        for (int d = lane; d <= tl1; d += 32) {
+            ga[d] = S.cnt[d];
+            gd[d] = (uint16_t)d;
+        }
         __syncwarp();
         if (lane == 0) {
-            top_quick_sort(S.cnt, S.diag, tl1, jlo);
+            top_quick_sort(ga, gd, tl1, jlo);
             for (int i = tl1 - 1; i >= jlo; --i)
-                if (S.cnt[i] > 0) {
-                    const int c = S.diag[i];
+                if (ga[i] > 0) {
+                    const int c = gd[i];
                     set_flags(S.flagw, max(1, c - P.window), min(tl1, c + P.window));
                 }
         }
@@ -604,6 +608,8 @@ struct cwgpu_fast_state {
     size_t smem_set = 0;
     uint2* d_ovf = nullptr;  // list overflow, ovf_records per warp of the grid
     size_t ovf_bytes = 0;
+    uint16_t* d_sort = nullptr;  // sort copies, 2 * sort_stride per warp of the grid
+    size_t sort_bytes = 0;
     // cwgpu_fast_align_pairs: grow-only pair, order and output arrays
     int32_t* d_pairs = nullptr;
     int32_t* d_order = nullptr;
@@ -615,7 +621,7 @@ struct cwgpu_fast_state {
 void cwgpu_fast_release(cwgpu_context* ctx) {
     if (!ctx || !ctx->fast) return;
     cwgpu_fast_state* F = ctx->fast;
-    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter, F->d_ovf,
+    void* ptrs[] = {F->d_orig, F->d_kcode, F->d_pos, F->d_start, F->d_counter, F->d_ovf, F->d_sort,
                     F->d_pairs, F->d_order, F->d_dist, F->d_stats};
     for (void* p : ptrs)
         if (p) cudaFree(p);
@@ -726,6 +732,15 @@ int run_fast(cwgpu_context* ctx, const Params& P, const int32_t* d_pairs, const 
         FAST_CUDA(ctx, cudaMalloc(&F->d_ovf, ovf));
         F->ovf_bytes = ovf;
     }
+    const long long sort_stride = 2LL * ctx->lmax + 4;
+    const size_t sortb = (size_t)grid * 2 * (size_t)sort_stride * sizeof(uint16_t);
+    if (sortb > F->sort_bytes) {
+        if (F->d_sort) FAST_CUDA(ctx, cudaFree(F->d_sort));
+        F->d_sort = nullptr;
+        F->sort_bytes = 0;
+        FAST_CUDA(ctx, cudaMalloc(&F->d_sort, sortb));
+        F->sort_bytes = sortb;
+    }
     Args A;
     A.kcode = F->d_kcode;
     A.pos = F->d_pos;
@@ -742,6 +757,8 @@ int run_fast(cwgpu_context* ctx, const Params& P, const int32_t* d_pairs, const 
     A.lmax = ctx->lmax;
     A.overflow = F->d_ovf;
     A.ovf_stride = ovf_records;
+    A.sortbuf = F->d_sort;
+    A.sort_stride = sort_stride;
     FAST_CUDA(ctx, cudaMemsetAsync(F->d_counter, 0, sizeof(unsigned long long), st));
     if (npairs > 0) {
         k_fast<<<(unsigned)grid, 32, sm, st>>>(A);
