@@ -59,7 +59,7 @@ struct Args {
     double* r;  // sumCols + sumRows of the valid nodes, for the search
     unsigned char* valid;
     int* rep;  // cycle that last formed the cluster node i stands for (0: leaf)
-    int* vlist;  // the valid nodes in ascending order (n + 1 entries)
+    int* vlist;  // two buffers of n + 1 entries: the valid nodes in ascending order
     unsigned long long* cand_k;  // order key of the criterion
     long long* cand_idx;
     int2* cand_ij;
@@ -293,6 +293,12 @@ struct ListTerms {  // x[list[k]]: the terms of the valid nodes only, in ascendi
     const int* list;
     __device__ double operator()(int k) const { return x[list[k]]; }
 };
+struct ListSkipTerms {  // the same with entry `skip` (a node that just left) read as +0.0
+    const double* x;
+    const int* list;
+    int skip;
+    __device__ double operator()(int k) const { return k == skip ? 0.0 : x[list[k]]; }
+};
 struct ColTerms {  // d(j, i) for i > j: column j of the packed triangle
     const double* d;
     int j;
@@ -309,14 +315,14 @@ struct Smem {
     long long* red_i;
     int2* red_ij;
     double* red_d;
-    double* ext;  // sumCols, sumRows, av, join (n+1 each), then rep and vlist (n+1 ints each)
+    double* ext;  // sumCols, sumRows, av, join (n+1 each), then rep and two lists (n+1 ints each)
 };
 
 __host__ __device__ inline size_t smem_layout(int n, bool node_shared, size_t* ext_off, size_t* v_off) {
     size_t off = sizeof(double) * (size_t)(n + 1);                          // r
     off += (2 * sizeof(double) + sizeof(long long) + sizeof(int2)) * kWarps;  // reduction scratch
     *ext_off = off;
-    if (node_shared) off += 4 * sizeof(double) * (size_t)(n + 1) + 2 * sizeof(int) * (size_t)(n + 1);
+    if (node_shared) off += 4 * sizeof(double) * (size_t)(n + 1) + 3 * sizeof(int) * (size_t)(n + 1);
     *v_off = off;
     return off + (size_t)(n + 1) + 16;
 }
@@ -351,6 +357,7 @@ struct Node {
     unsigned char* valid;
     int* rep;
     int* vlist;  // valid nodes, ascending: the terms of the sequential sums
+    int* vnext;  // the other list buffer (the list without this cycle's minj)
 };
 
 // A search candidate: criterion, element index (scan order), (ii, jj) and
@@ -494,8 +501,35 @@ __device__ void publish_r(const Args& A, const Node& N, bool shared, int t0, int
     }
 }
 
+// Branch lengths of cycle nc (NJTree.cpp:378-470), av and rep of the joined
+// node. Nothing else in the cycle reads what this writes, so one thread does
+// it beside the sums.
+__device__ void branch_lengths(const Args& A, const Node& N, int nc, int mini, int minj, double dmin, double dio_sum,
+                               double djo_sum, double avi, double avj) {
+    const double fnseqs = A.scal[2];
+    const double fnseqs2 = A.scal[1];
+    const double dio = __ddiv_rn(__dsub_rn(dio_sum, dmin), fnseqs2);
+    const double djo = __ddiv_rn(__dsub_rn(djo_sum, dmin), fnseqs2);
+    double bi = __dmul_rn(__dsub_rn(__dadd_rn(dmin, dio), djo), 0.5);
+    double bj = __dsub_rn(dmin, bi);
+    bi = __dsub_rn(bi, avi);
+    bj = __dsub_rn(bj, avj);
+    if (fabs(bi) < 0.0001) bi = 0.0;
+    if (fabs(bj) < 0.0001) bj = 0.0;
+    A.left[nc] = bi;
+    A.right[nc] = bj;
+    if (dmin <= 0.0) dmin = 0.000001;
+    N.av[mini] = __dmul_rn(dmin, 0.5);
+    A.scal[2] = __dsub_rn(fnseqs, 1.0);
+    N.rep[mini] = nc;
+    if (A.joins) {
+        A.joins[2 * (nc - 1)] = mini;
+        A.joins[2 * (nc - 1) + 1] = minj;
+    }
+}
+
 // One join (CTA 0): NJTree.cpp:378-641 as restated in the oracle.
-__device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
+__device__ bool update(const Args& A, Node& N, bool shared, int nc) {
     const int n = A.n;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ int s_mini, s_minj, s_repi, s_repj;
@@ -549,30 +583,6 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
         return false;
     }
     const int typei = s_avi > 0.0 ? 0 : 1, typej = s_avj > 0.0 ? 0 : 1;
-    if (threadIdx.x == 0) {
-        // Branch lengths (NJTree.cpp:378-470).
-        const double fnseqs = A.scal[2];
-        const double fnseqs2 = A.scal[1];
-        double dmin = s_dmin;
-        const double dio = __ddiv_rn(__dsub_rn(s_dio, dmin), fnseqs2);
-        const double djo = __ddiv_rn(__dsub_rn(s_djo, dmin), fnseqs2);
-        double bi = __dmul_rn(__dsub_rn(__dadd_rn(dmin, dio), djo), 0.5);
-        double bj = __dsub_rn(dmin, bi);
-        bi = __dsub_rn(bi, s_avi);
-        bj = __dsub_rn(bj, s_avj);
-        if (fabs(bi) < 0.0001) bi = 0.0;
-        if (fabs(bj) < 0.0001) bj = 0.0;
-        A.left[nc] = bi;
-        A.right[nc] = bj;
-        if (dmin <= 0.0) dmin = 0.000001;
-        N.av[mini] = __dmul_rn(dmin, 0.5);
-        A.scal[2] = __dsub_rn(fnseqs, 1.0);
-        N.rep[mini] = nc;
-        if (A.joins) {
-            A.joins[2 * (nc - 1)] = mini;
-            A.joins[2 * (nc - 1) + 1] = minj;
-        }
-    }
     // treeDesc row nc (NJTree.cpp:478-531) and the joined row (NJTree.cpp:541-641),
     // one node per thread: each node's sums, join value and matrix entries are
     // touched only by its own iteration, so the reference's two loops fuse.
@@ -615,7 +625,8 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
     // minj leaves the list of valid nodes (nv of them before this join: one
     // node leaves per cycle). The reference's sums run over the valid nodes in
     // ascending order, skipping the others, which add +0.0 and change nothing,
-    // so the sums below walk the list instead of all n nodes.
+    // so the sums below walk the list instead of all n nodes. The list
+    // without minj is written to the other buffer beside the first sums.
     const int nv = n - nc + 1;
     __shared__ int s_pi, s_pj, s_bad;
     if (threadIdx.x == 0) {
@@ -636,35 +647,33 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
     }
     __syncthreads();
     if (s_bad) return false;
-    const int pi = s_pi;
-    for (int b0 = s_pj; b0 < nv - 1; b0 += blockDim.x) {  // vlist[pj+1 .. nv) down one
-        const int k = b0 + (int)threadIdx.x;
-        const int v = k < nv - 1 ? N.vlist[k + 1] : 0;
-        __syncthreads();
-        if (k < nv - 1) N.vlist[k] = v;
-        __syncthreads();
-    }
+    const int pi = s_pi, pj = s_pj;
     // The reference's three sequential sums on three warps (three SM
     // sub-partitions): sumRows[mini] and sumCols[mini] over the joined row
     // (NJTree.cpp:590-616) and the next cycle's sumd over sumCols
     // (NJTree.cpp:314-321), whose terms after mini wait for sumCols[mini].
-    // The other warps meanwhile form the next search's diq/djq terms.
+    // The other warps meanwhile form the next search's diq/djq terms, the
+    // list without minj and the branch lengths.
     double sumd_part = 0.0;
     if (warp == 0) {
         const double v = warp_seq_sum(ListTerms{N.join, N.vlist}, 0, pi, 0.0);
         if (lane == 0) s_sR = v;
     } else if (warp == 1) {
-        const double v = warp_seq_sum(ListTerms{N.join, N.vlist}, pi + 1, nv - 1, 0.0);
+        const double v = warp_seq_sum(ListSkipTerms{N.join, N.vlist, pj}, pi + 1, nv, 0.0);
         if (lane == 0) s_sC = v;
     } else if (warp == 2) {
         sumd_part = warp_seq_sum(ListTerms{N.sumCols, N.vlist}, 0, pi, 0.0);
     } else {
+        if (threadIdx.x == 96)
+            branch_lengths(A, N, nc, mini, minj, s_dmin, s_dio, s_djo, s_avi, s_avj);
+        for (int k = (int)threadIdx.x - 96; k < nv - 1; k += blockDim.x - 96)
+            N.vnext[k] = N.vlist[k < pj ? k : k + 1];
         publish_r(A, N, shared, 96, mini);
     }
     __syncthreads();
     if (warp == 2) {
         double v = __dadd_rn(sumd_part, s_sC);
-        v = warp_seq_sum(ListTerms{N.sumCols, N.vlist}, pi + 1, nv - 1, v);
+        v = warp_seq_sum(ListTerms{N.sumCols, N.vnext}, pi + 1, nv - 1, v);
         if (lane == 0) s_sumd = v;
     }
     __syncthreads();
@@ -681,6 +690,9 @@ __device__ bool update(const Args& A, const Node& N, bool shared, int nc) {
         A.scal[1] = __dsub_rn(fnseqs, 2.0);
     }
     __syncthreads();
+    int* const t = N.vlist;  // the next cycle reads the list without minj
+    N.vlist = N.vnext;
+    N.vnext = t;
     return true;
 }
 
@@ -772,6 +784,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nj(Args A) {
         N.join = S.ext + 3 * (size_t)(n + 1);
         N.rep = reinterpret_cast<int*>(S.ext + 4 * (size_t)(n + 1));
         N.vlist = N.rep + (n + 1);
+        N.vnext = N.vlist + (n + 1);
         N.r = S.r;
         N.valid = S.v;
         for (int j = threadIdx.x; j <= n; j += blockDim.x) {
@@ -783,7 +796,7 @@ __global__ void __launch_bounds__(kThreads, 1) k_nj(Args A) {
             N.valid[j] = j > 0;
         }
     } else {
-        N = Node{A.sumCols, A.sumRows, A.av, A.join, A.r, A.valid, A.rep, A.vlist};
+        N = Node{A.sumCols, A.sumRows, A.av, A.join, A.r, A.valid, A.rep, A.vlist, A.vlist + (n + 1)};
     }
     for (int k = threadIdx.x; k < n; k += blockDim.x) N.vlist[k] = k + 1;  // every node starts valid
     __syncthreads();
@@ -900,7 +913,7 @@ int ensure(cwgpu_nj* h, int n) {
         NJ_CHECK(h, cudaMalloc(&h->d_joins, (size_t)2 * (n + 1) * sizeof(int)));
         NJ_CHECK(h, cudaMalloc(&h->d_vec, 5 * (size_t)(n + 1) * sizeof(double)));
         NJ_CHECK(h, cudaMalloc(&h->d_valid, (size_t)(n + 1)));
-        NJ_CHECK(h, cudaMalloc(&h->d_rep, 2 * (size_t)(n + 1) * sizeof(int)));  // rep, then the valid list
+        NJ_CHECK(h, cudaMalloc(&h->d_rep, 3 * (size_t)(n + 1) * sizeof(int)));  // rep, then two valid lists
         h->cap_n = n;
     }
     const size_t sm = smem_bytes(n, node_shared_for(h, n));
