@@ -73,6 +73,13 @@ def test_gpu_nj_matches_oracle_seeded(nj, oracle_mod, n, seed, ties):
     check(nj, oracle_mod, n, random_matrix(n, seed, ties))
 
 
+def test_gpu_nj_node_arrays_in_global_memory(nj, oracle_mod):
+    """Above about 4,370 sequences CTA 0's per-node arrays (sums, joins, the
+    two lists of valid nodes) no longer fit shared memory and live in global
+    memory; the tree is still the oracle's."""
+    check(nj, oracle_mod, 4400, random_matrix(4400, 9))
+
+
 def test_gpu_nj_first_join_is_first_minimum(nj):
     """The first cycle's join is the first minimum of the criterion in the
     reference's scan order, recomputed here in float64 with the same
