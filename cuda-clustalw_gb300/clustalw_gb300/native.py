@@ -184,6 +184,7 @@ SIGNATURES = {
     "cwgpu_nj_tree_device": (ctypes.c_int, [_vp, _i32, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "cwgpu_nj_last_stats": (ctypes.c_int, [_vp, ctypes.POINTER(_i64), ctypes.POINTER(ctypes.c_double)]),
     "cwgpu_nj_seq_sum": (ctypes.c_int, [_vp, _vp, _i64, ctypes.c_double, ctypes.POINTER(ctypes.c_double)]),
+    "cwgpu_nj_wait_probe": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(ctypes.c_int32)]),
 }
 
 _lib = None

@@ -100,6 +100,15 @@ class NJGpu:
             raise self._err(rc, "cwgpu_nj_seq_sum")
         return out.value
 
+    def wait_probe(self, timeout_ns):
+        """The tree kernel's bounded wait on a counter nothing raises: True
+        when it ended at its limit with the timeout status."""
+        out = ctypes.c_int32()
+        rc = self._lib.cwgpu_nj_wait_probe(self._h, int(timeout_ns), ctypes.byref(out))
+        if rc:
+            raise self._err(rc, "cwgpu_nj_wait_probe")
+        return bool(out.value)
+
     def last_stats(self):
         p = ctypes.c_int64()
         s = ctypes.c_double()

@@ -71,6 +71,7 @@ struct Args {
     unsigned* release;  // cycles CTA 0 has published
     int* status;
     bool node_shared;   // CTA 0 keeps the per-node arrays in shared memory
+    unsigned long long wait_ns;  // limit of every wait between CTAs
 };
 
 __device__ __forceinline__ size_t tri(int a) { return ((size_t)a * (size_t)(a + 1)) >> 1; }
@@ -396,7 +397,7 @@ __device__ bool wait_geq(const Args& A, const unsigned* p, unsigned target) {
         unsigned it = 0;
         while ((int)(ld_acquire(p) - target) < 0) {
             if (ld_status(A.status) != ST_OK) break;
-            if (++it > kSpinLimit || gtimer() - t0 > kBarrierTimeoutNs) {
+            if (++it > kSpinLimit || gtimer() - t0 > A.wait_ns) {
                 atomicCAS(A.status, ST_OK, ST_TIMEOUT);
                 break;
             }
@@ -826,6 +827,10 @@ __global__ void __launch_bounds__(kThreads, 1) k_nj(Args A) {
     last_cycle(A, N);
 }
 
+// Diagnostic: one CTA waits, with the tree's wait, for a counter that nothing
+// raises; the wait must end at its limit with ST_TIMEOUT.
+__global__ void k_wait_probe(Args A, unsigned target) { wait_geq(A, A.arrive, target); }
+
 // One warp replays s0 + x[0] + ... + x[count-1] (diagnostic entry point).
 __global__ void k_seq_sum(const double* x, int count, double s0, double* out) {
     const double v = warp_seq_sum(PlainTerms{x}, 0, count, s0);
@@ -981,6 +986,7 @@ int run(cwgpu_nj* h, int n, cudaStream_t st, double* d_left, double* d_right, in
     A.release = h->d_sig + 1;
     A.status = h->d_status;
     A.node_shared = node_shared_for(h, n);
+    A.wait_ns = kBarrierTimeoutNs;
     void* args[] = {&A};
     NJ_CHECK(h, cudaEventRecord(h->ev0, st));
     NJ_CHECK(h, cudaLaunchCooperativeKernel((const void*)k_nj, dim3(h->grid), dim3(kThreads), args,
@@ -1108,6 +1114,27 @@ int cwgpu_nj_tree_device(cwgpu_nj* h, int32_t n, const double* d_elements_in, do
         NJ_CHECK(h, cudaMemcpyAsync(d_elements_out, h->d_work, nel * sizeof(double), cudaMemcpyDeviceToDevice, st));
     NJ_CHECK(h, cudaStreamSynchronize(st));
     return finish(h, n);
+}
+
+int cwgpu_nj_wait_probe(cwgpu_nj* h, int64_t timeout_ns, int32_t* timed_out) {
+    if (!h || !timed_out || timeout_ns <= 0 || timeout_ns > (int64_t)kBarrierTimeoutNs) return CWGPU_ERR_ARG;
+    NJ_CHECK(h, cudaSetDevice(h->device));
+    NJ_CHECK(h, cudaMemsetAsync(h->d_sig, 0, 2 * sizeof(unsigned), h->stream));
+    NJ_CHECK(h, cudaMemsetAsync(h->d_status, 0, sizeof(int), h->stream));
+    Args A;
+    memset(&A, 0, sizeof(A));
+    A.arrive = h->d_sig;
+    A.release = h->d_sig + 1;
+    A.status = h->d_status;
+    A.wait_ns = (unsigned long long)timeout_ns;
+    k_wait_probe<<<1, 32, 0, h->stream>>>(A, 1u);
+    NJ_CHECK(h, cudaGetLastError());
+    NJ_CHECK(h, cudaStreamSynchronize(h->stream));
+    int status = 0;
+    NJ_CHECK(h, cudaMemcpy(&status, h->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+    NJ_CHECK(h, cudaMemset(h->d_status, 0, sizeof(int)));
+    *timed_out = status == ST_TIMEOUT ? 1 : 0;
+    return CWGPU_OK;
 }
 
 int cwgpu_nj_seq_sum(cwgpu_nj* h, const double* x, int64_t count, double s0, double* out) {

@@ -76,6 +76,12 @@ int cwgpu_nj_last_stats(const cwgpu_nj* nj, int64_t* pairs_evaluated, double* ke
  * same routine; this entry point lets tests feed it adversarial terms. */
 int cwgpu_nj_seq_sum(cwgpu_nj* nj, const double* x, int64_t count, double s0, double* out);
 
+/* Diagnostic: runs the tree kernel's wait between CTAs on a counter that
+ * nothing raises, limited to timeout_ns (1 .. 4e9). *timed_out is 1 when the
+ * wait ended at its limit with the timeout status, as every such wait must;
+ * the handle stays usable. No GPU fault or hang is involved. */
+int cwgpu_nj_wait_probe(cwgpu_nj* nj, int64_t timeout_ns, int32_t* timed_out);
+
 #ifdef __cplusplus
 }
 #endif

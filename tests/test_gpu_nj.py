@@ -80,6 +80,18 @@ def test_gpu_nj_node_arrays_in_global_memory(nj, oracle_mod):
     check(nj, oracle_mod, 4400, random_matrix(4400, 9))
 
 
+def test_gpu_nj_bounded_wait_ends_with_timeout_status(nj, oracle_mod):
+    """A wait between CTAs whose counter nothing raises ends at its limit
+    (here 2 ms) with the timeout status instead of hanging, and the handle
+    still builds a correct tree afterwards."""
+    import time
+
+    t = time.perf_counter()
+    assert nj.wait_probe(2_000_000)
+    assert time.perf_counter() - t < 5.0
+    check(nj, oracle_mod, 40, random_matrix(40, 12))
+
+
 def test_gpu_nj_first_join_is_first_minimum(nj):
     """The first cycle's join is the first minimum of the criterion in the
     reference's scan order, recomputed here in float64 with the same
