@@ -262,7 +262,7 @@ def reference_arm(args):
 
 
 def served_leg(args, matrix, params, device):
-    """BASELINE-style served stream: Poisson arrivals of independent protein
+    """Served stream: Poisson arrivals of independent protein
     families (sequence count U[10, 500], root length U[50, 1500]) admitted
     under a 40 GB budget and mixed in shared rounds; p50/p99 job latency and
     throughput, next to the plain form that runs the same jobs one at a time."""
