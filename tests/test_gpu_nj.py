@@ -269,3 +269,6 @@ def test_gpu_sequential_sum_replay(nj, seed):
     for count in range(0, 70):
         x = np.random.default_rng(count).uniform(0, 1, count)
         assert nj.seq_sum(x) == seq(x)
+    # a long sum of float32-valued terms (ties and late rounding)
+    x = np.random.default_rng(seed).uniform(0, 1, 9000).astype(np.float32).astype(np.float64)
+    assert np.float64(nj.seq_sum(x, 0.3)).view(np.int64) == np.float64(seq(x, 0.3)).view(np.int64)

@@ -204,3 +204,26 @@ def test_autotune_picks_all_knobs(ctx):
     assert len({c[2] for c in timings}) >= 2  # short-pair thresholds were timed
     assert np.array_equal(ctx.align_pairs(pairs), before)
     ctx.set_tuning(32, 16, 128)
+
+
+def test_short_pair_kernel_dna(ctx, oracle_mod):
+    """DNA (IUB, dense alphabet of 4-5 codes) through the 4-row kernel:
+    a family of ~100 residues, every pair short."""
+    from clustalw_gb300 import load_matrix, synth
+
+    matrix, params = load_matrix("dna")
+    seqs = synth.dna_family(30, 100, seed=21)
+    assert max(len(s) for s in seqs) <= 128
+    ctx.set_matrix(matrix)
+    ctx.set_params(params)
+    ctx.upload_seqs(seqs)
+    pairs = range_pairs(len(seqs), 0, len(seqs), 0, len(seqs))
+    plan = ctx.plan(pairs)
+    assert plan.kernel_count() == 1
+    plan.launch()
+    dist, st = plan.results(stats=True)
+    plan.close()
+    want = oracle_mod.align_pairs(seqs, matrix, params, pairs)
+    assert np.array_equal(dist, want["dist"])
+    for f in STAT_FIELDS:
+        assert np.array_equal(st[f], want[f]), f
