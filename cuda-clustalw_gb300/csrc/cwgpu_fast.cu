@@ -305,17 +305,22 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     int T = 0;
     if (kk > 0) {
         int cur = 0x7fffffff, got = 0, eq = 0;
-        for (;;) {  // k-th largest of cnt[1..tl1-1], with multiplicity
-            int v = -1;
+        for (;;) {  // k-th largest of cnt[1..tl1-1], with multiplicity: one scan per distinct value
+            int lv = -1, lc = 0;  // this lane's largest count below cur and how often it occurs
             for (int d = 1 + lane; d <= tl1 - 1; d += 32) {
                 const int x = S.cnt[d];
-                if (x < cur) v = max(v, x);
+                if (x < cur) {
+                    if (x > lv) {
+                        lv = x;
+                        lc = 1;
+                    } else if (x == lv) {
+                        ++lc;
+                    }
+                }
             }
-            v = warp_max(v);
+            const int v = warp_max(lv);
             if (v < 0) break;  // fewer than kk values below cur (cannot happen: kk <= tl1 - 1)
-            int c = 0;
-            for (int d = 1 + lane; d <= tl1 - 1; d += 32) c += S.cnt[d] == v;
-            c = warp_sum(c);
+            const int c = warp_sum(lv == v ? lc : 0);
             got += c;
             cur = v;
             if (got >= kk) {
