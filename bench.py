@@ -304,6 +304,12 @@ def served_leg(args, matrix, params, device):
             srv.wait(jid)
             srv.release(jid)
         burst_s = time.perf_counter() - t
+    # The same arrivals under the least-remaining-work-first policy.
+    with Server(matrix, params, device=device, memory_budget=40 << 30, max_seq_len=2048, round_cells=6e9,
+                policy="srpt") as srv:
+        for k in range(2):
+            srv.wait(srv.submit(packed=jobs[k]))
+        lat_srpt, _, _ = run_arrivals(srv, jobs, args.serve_rate, seed=args.seed)
     return {
         "rate_jobs_per_s": args.serve_rate,
         "jobs": njobs,
@@ -316,6 +322,9 @@ def served_leg(args, matrix, params, device):
         "plain_per_job_gcups": c_plain / t_plain / 1e9,
         "plain_sample_jobs": len(sample),
         "rounds": info["rounds"],
+        "policy": "fifo (admission order)",
+        "srpt": {"p50_ms": 1e3 * percentile(lat_srpt, 50), "p99_ms": 1e3 * percentile(lat_srpt, 99),
+                 "mean_ms": 1e3 * float(np.mean(lat_srpt)), "policy": "least remaining work first"},
         "budget_bytes": 40 << 30,
         "workload": "protein families, N ~ U[10,500], root length ~ U[50,1500], Poisson arrivals",
     }

@@ -106,6 +106,8 @@ class ServerOpts(ctypes.Structure):
         ("max_seq_len", ctypes.c_int32),
         ("round_cells", ctypes.c_double),
         ("max_items_per_round", ctypes.c_int64),
+        ("policy", ctypes.c_int32),
+        ("reserved", ctypes.c_int32),
     ]
 
 

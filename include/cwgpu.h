@@ -223,7 +223,14 @@ typedef struct cwgpu_server_opts {
     int32_t max_seq_len;         /* longest sequence a job may hold */
     double round_cells;          /* sum of n*m per round (work granularity) */
     int64_t max_items_per_round; /* pairs per round */
+    int32_t policy;              /* order jobs fill a round in: CWGPU_SERVE_FIFO or CWGPU_SERVE_SRPT */
+    int32_t reserved;            /* 0 */
 } cwgpu_server_opts;
+/* CWGPU_SERVE_FIFO: admission order (the default; best p99 on the mixes
+ * measured). CWGPU_SERVE_SRPT: the job with the least remaining work first
+ * (about half the p50 and a lower mean, a higher p99). Results never depend
+ * on the policy. */
+enum { CWGPU_SERVE_FIFO = 0, CWGPU_SERVE_SRPT = 1 };
 typedef struct cwgpu_server_stats {
     int64_t jobs_queued, jobs_running, jobs_done;
     int64_t rounds, pairs;

@@ -31,7 +31,8 @@ def protein_jobs():
     return [synth.protein_family(n, L, s) for n, L, s in spec]
 
 
-def test_mixed_jobs_equal_alone():
+@pytest.mark.parametrize("policy", ["fifo", "srpt"])
+def test_mixed_jobs_equal_alone(policy):
     from clustalw_gb300 import load_matrix
     from clustalw_gb300.serve import Server
 
@@ -39,7 +40,7 @@ def test_mixed_jobs_equal_alone():
     jobs = protein_jobs()
     want = [alone(matrix, params, j) for j in jobs]
     # Small rounds so every round mixes pairs of several jobs.
-    with Server(matrix, params, memory_budget=256 << 20, round_cells=2e6) as srv:
+    with Server(matrix, params, memory_budget=256 << 20, round_cells=2e6, policy=policy) as srv:
         ids = [srv.submit(j, stats=True) for j in jobs]
         for jid in ids:
             srv.wait(jid, timeout_ms=120000)
