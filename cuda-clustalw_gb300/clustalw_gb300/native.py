@@ -107,7 +107,7 @@ class ServerOpts(ctypes.Structure):
         ("round_cells", ctypes.c_double),
         ("max_items_per_round", ctypes.c_int64),
         ("policy", ctypes.c_int32),
-        ("reserved", ctypes.c_int32),
+        ("srpt_age_ms", ctypes.c_int32),
     ]
 
 

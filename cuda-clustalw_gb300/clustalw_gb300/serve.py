@@ -23,13 +23,15 @@ class Server:
     POLICIES = {"fifo": 0, "srpt": 1}
 
     def __init__(self, matrix, params, device=0, memory_budget=8 << 30, max_jobs=256, max_seq_len=4096,
-                 round_cells=4e9, max_items_per_round=1 << 20, policy="fifo"):
-        """policy: "fifo" (admission order) or "srpt" (least remaining work first)."""
+                 round_cells=4e9, max_items_per_round=1 << 20, policy="srpt", srpt_age_ms=500):
+        """policy: "srpt" (least remaining work first; jobs older than
+        srpt_age_ms, if > 0, go first in admission order) or "fifo" (admission
+        order)."""
         self._lib = native.load()
         m = np.ascontiguousarray(np.asarray(matrix, dtype=np.int32).reshape(-1))
         p = params if isinstance(params, Params) else Params.from_dict(params)
         opts = ServerOpts(int(memory_budget), int(max_jobs), int(max_seq_len), float(round_cells),
-                          int(max_items_per_round), self.POLICIES[policy], 0)
+                          int(max_items_per_round), self.POLICIES[policy], int(srpt_age_ms))
         h = ctypes.c_void_p()
         rc = self._lib.cwgpu_server_create(int(device), m.ctypes.data, ctypes.byref(p), ctypes.byref(opts),
                                            ctypes.byref(h))

@@ -351,11 +351,17 @@ int64_t build_round(cwgpu_server* s, Round& r, WorkItem* out) {
     for (Job* j : s->admitted)
         if (j->scheduled < j->npairs) order.push_back(j);
     if (s->opts.policy == CWGPU_SERVE_SRPT) {
+        // Least remaining work first; jobs older than the age cap go first, in
+        // admission order (the sort is stable).
+        const double now = now_s(), cap = s->opts.srpt_age_ms > 0 ? 1e-3 * s->opts.srpt_age_ms : 1e300;
         auto remaining = [](const Job* j) {
             return (double)j->cells_nm * (double)(j->npairs - j->scheduled) / (double)std::max<int64_t>(j->npairs, 1);
         };
-        std::stable_sort(order.begin(), order.end(),
-                         [&](const Job* a, const Job* b) { return remaining(a) < remaining(b); });
+        std::stable_sort(order.begin(), order.end(), [&](const Job* a, const Job* b) {
+            const bool oa = now - a->t_submit > cap, ob = now - b->t_submit > cap;
+            if (oa != ob) return oa;
+            return !oa && remaining(a) < remaining(b);
+        });
     }
     double budget = s->opts.round_cells;
     int64_t n = 0;
@@ -538,7 +544,7 @@ int cwgpu_server_create(int device, const int32_t* matrix, const cwgpu_params* p
     *out = nullptr;
     if (opts->memory_budget_bytes <= 0 || opts->max_jobs <= 0 || opts->max_seq_len <= 0 ||
         opts->max_seq_len > CWGPU_MAX_SEQ_LEN || opts->round_cells <= 0 || opts->max_items_per_round <= 0 ||
-        (opts->policy != CWGPU_SERVE_FIFO && opts->policy != CWGPU_SERVE_SRPT))
+        (opts->policy != CWGPU_SERVE_FIFO && opts->policy != CWGPU_SERVE_SRPT) || opts->srpt_age_ms < 0)
         return CWGPU_ERR_ARG;
     for (int i = 0; i < CWGPU_NUMRES * CWGPU_NUMRES; ++i)
         if (matrix[i] < -32768 || matrix[i] > 32767) return CWGPU_ERR_MATRIX;

@@ -31,8 +31,8 @@ def protein_jobs():
     return [synth.protein_family(n, L, s) for n, L, s in spec]
 
 
-@pytest.mark.parametrize("policy", ["fifo", "srpt"])
-def test_mixed_jobs_equal_alone(policy):
+@pytest.mark.parametrize("policy,age", [("fifo", 0), ("srpt", 0), ("srpt", 1)])
+def test_mixed_jobs_equal_alone(policy, age):
     from clustalw_gb300 import load_matrix
     from clustalw_gb300.serve import Server
 
@@ -40,7 +40,7 @@ def test_mixed_jobs_equal_alone(policy):
     jobs = protein_jobs()
     want = [alone(matrix, params, j) for j in jobs]
     # Small rounds so every round mixes pairs of several jobs.
-    with Server(matrix, params, memory_budget=256 << 20, round_cells=2e6, policy=policy) as srv:
+    with Server(matrix, params, memory_budget=256 << 20, round_cells=2e6, policy=policy, srpt_age_ms=age) as srv:
         ids = [srv.submit(j, stats=True) for j in jobs]
         for jid in ids:
             srv.wait(jid, timeout_ms=120000)
