@@ -142,9 +142,10 @@ int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t np
  * A plan uploads a pair list and its load-balancing order (longest pairs
  * first) once, owns device output arrays and holds a CUDA graph of the
  * persistent launch, so repeated runs over resident inputs cost one
- * cudaGraphLaunch. Pairs whose first sequence has at most 128 residues run in
- * a second persistent kernel (4 rows per lane instead of 8) inside the same
- * graph, beside the long-pair kernel at lower priority. A plan is tied to the sequences, matrix and params that were
+ * cudaGraphLaunch. Pairs whose first sequence has at most
+ * cwgpu_tuning.short_rows residues (128 by default) run in a second
+ * persistent kernel (4 rows per lane instead of 8) inside the same graph,
+ * beside the long-pair kernel at lower priority. A plan is tied to the sequences, matrix and params that were
  * current when it was made: after cwgpu_upload_seqs/set_params/set_matrix,
  * cwgpu_plan_launch returns CWGPU_ERR_STATE. Plans of one context share its
  * scratch memory and must not run concurrently. No reference counterpart: the
