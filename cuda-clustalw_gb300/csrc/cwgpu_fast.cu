@@ -268,21 +268,12 @@ __device__ __forceinline__ void set_flags(unsigned* flagw, int lo, int hi) {
     for (int l = lo; l <= hi; ++l) atomicOr(&flagw[l >> 5], 1u << (l & 31));
 }
 
-// One pair on one warp.
-__device__ void fast_pair(const Args& A, const Smem& S, long long q) {
-    const Params& P = A.P;
+// Hits per diagonal (:198-219) into 16-bit counts (at most min(l1, l2)),
+// cnt[0 .. tl1+1].
+__device__ __forceinline__ void count_hits(const Smem& S, const int16_t* kc1, const uint16_t* pos2,
+                                           const int32_t* st2, int l1, int l2, int ktup) {
     const int lane = threadIdx.x & 31;
-    const int si = A.pairs[2 * q], sj = A.pairs[2 * q + 1];
-    const int l1 = A.lens[si], l2 = A.lens[sj];
-    const int64_t o1 = A.offs[si], o2 = A.offs[sj];
     const int tl1 = l1 + l2 - 1;
-    const int ktup = P.ktup;
-    const int16_t* kc1 = A.kcode + o1;
-    const int16_t* kc2 = A.kcode + o2;  // kc2[p - 1]: code of the k-tuple at 1-based p of seq 2
-    const uint16_t* pos2 = A.pos + o2;
-    const int32_t* st2 = A.start + (size_t)sj * (P.limit + 2);
-
-    // ---- count hits per diagonal (:198-219), 16-bit counts (at most min(l1, l2))
     const int ncw = (tl1 + 3) / 2;  // words holding counts 0..tl1+1
     for (int w = lane; w < ncw; w += 32) S.cntw[w] = 0;
     __syncwarp();
@@ -298,7 +289,13 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     }
     __syncwarp();
 
-    // ---- select the top diagonals (:221-241)
+}
+
+// The top diagonals (:221-241), the diagonals within `window` of them flagged,
+// and the flagged diagonals in ascending order in S.flagged; returns how many.
+__device__ __forceinline__ int flag_top_diagonals(const Args& A, const Smem& S, int tl1) {
+    const Params& P = A.P;
+    const int lane = threadIdx.x & 31;
     const int jlo = max(1, tl1 - P.signif + 1);  // first top position
     const int kk = tl1 - jlo;                    // sorted top positions jlo..tl1-1
     int mode = 0;                                 // 0: none, 1: count > T, 2: count >= T, 3: sorted
@@ -380,19 +377,35 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
     for (int f = lane; f < nf; f += 32) S.last[f] = 0;
     __syncwarp();
 
-    // ---- chain fragments (:246-398), the whole warp together.
-    // The reference keeps every fragment in a list sorted by score (putFrag)
-    // and, for each match on a flagged diagonal, walks the list from the best
-    // fragment to the first one the match can follow (the A-loop). Here list
-    // entries are records (v1 | v2 << 16, score); the index of the entry at
-    // distance d from the head (maxSoFar) is nfr-1-d. The top 32 entries live
-    // in registers, lane d holding distance d (wf = 1, positions wv, score
-    // ws); indices [base, nfr-32) are the shared records sl[0 .. nsl) and
-    // indices below base the warp's global overflow array G. A walk from the
-    // head is a register test and then 32-wide scans down the rest. putFrag
-    // inserts close to the head: within the top 32 it is a register shift
-    // whose last entry joins the shared records; deeper it shifts the records
-    // above it. When the shared records are full, their lower half moves to G.
+    return nf;
+}
+
+struct ChainResult {
+    int nfr;         // fragments in the list
+    int frags;       // currFrag, the fragment count the reference reports
+    bool partial;    // the reference's "(Partial alignment)" cut-off was reached
+    int head_score;  // score of the best fragment (maxSoFar)
+};
+
+// Fragment chaining (:246-398), the whole warp together, over the nf flagged
+// diagonals in S.flagged.
+// The reference keeps every fragment in a list sorted by score (putFrag)
+// and, for each match on a flagged diagonal, walks the list from the best
+// fragment to the first one the match can follow (the A-loop). Here list
+// entries are records (v1 | v2 << 16, score); the index of the entry at
+// distance d from the head (maxSoFar) is nfr-1-d. The top 32 entries live
+// in registers, lane d holding distance d (wf = 1, positions wv, score
+// ws); indices [base, nfr-32) are the shared records sl[0 .. nsl) and
+// indices below base the warp's global overflow array G. A walk from the
+// head is a register test and then 32-wide scans down the rest. putFrag
+// inserts close to the head: within the top 32 it is a register shift
+// whose last entry joins the shared records; deeper it shifts the records
+// above it. When the shared records are full, their lower half moves to G.
+__device__ __forceinline__ ChainResult chain_fragments(const Args& A, const Smem& S, const int16_t* kc1,
+                                                       const int16_t* kc2, int l1, int l2, int nf) {
+    const Params& P = A.P;
+    const int lane = threadIdx.x & 31;
+    const int ktup = P.ktup;
     uint2* const G = A.overflow + (size_t)blockIdx.x * (size_t)A.ovf_stride;
     const int cap = S.cap;
     int nfr = 0, currFrag = 0, base = 0, nsl = 0;
@@ -560,7 +573,27 @@ __device__ void fast_pair(const Args& A, const Smem& S, long long q) {
             }
         }
     }
-    const int head_score = __shfl_sync(kFull, ws, 0);
+    return ChainResult{nfr, currFrag, partial, __shfl_sync(kFull, ws, 0)};
+}
+
+// One pair on one warp.
+__device__ void fast_pair(const Args& A, const Smem& S, long long q) {
+    const Params& P = A.P;
+    const int lane = threadIdx.x & 31;
+    const int si = A.pairs[2 * q], sj = A.pairs[2 * q + 1];
+    const int l1 = A.lens[si], l2 = A.lens[sj];
+    const int64_t o1 = A.offs[si], o2 = A.offs[sj];
+    const int tl1 = l1 + l2 - 1;
+    const int16_t* kc1 = A.kcode + o1;
+    const int16_t* kc2 = A.kcode + o2;  // kc2[p - 1]: code of the k-tuple at 1-based p of seq 2
+    const uint16_t* pos2 = A.pos + o2;
+    const int32_t* st2 = A.start + (size_t)sj * (P.limit + 2);
+
+    count_hits(S, kc1, pos2, st2, l1, l2, P.ktup);
+    const int nf = flag_top_diagonals(A, S, tl1);
+    const ChainResult ch = chain_fragments(A, S, kc1, kc2, l1, l2, nf);
+    const int nfr = ch.nfr, currFrag = ch.frags, head_score = ch.head_score;
+    const bool partial = ch.partial;
 
     // ---- distance (:88-103), in double as the reference
     if (lane == 0) {
