@@ -78,3 +78,44 @@ def test_autotune_helpers_cpu():
     assert work.min() < np.median(lens) ** 2 < work.max()
     assert autotune.length_profile(lens) == autotune.length_profile(lens.copy())
     assert autotune.length_profile([1523] * 10) != autotune.length_profile([97] * 10)
+
+
+def test_autotune_search_and_cache_cpu(tmp_path, monkeypatch):
+    """The tuner's search on a stand-in context with a known cost model: the
+    tiny-frame candidates first, then only the short-pair thresholds that
+    split the sample differently, the fastest kept and cached."""
+    from clustalw_gb300 import autotune, synth
+
+    class FakeCtx:
+        def __init__(self):
+            self.t = (32, 16, 128)
+            self.timed = []
+
+        def set_tuning(self, m, n, r=None):
+            self.t = (m, n, self.t[2] if r is None else r)
+
+        def get_tuning(self):
+            return self.t
+
+    def cost(t):  # best at (16, 16) and 192 rows
+        return abs(t[0] - 16) + abs(t[1] - 16) + abs(t[2] - 192) / 64 + 1.0
+
+    def fake_time(ctx, sample, repeats):
+        ctx.timed.append(ctx.t)
+        return cost(ctx.t)
+
+    monkeypatch.setattr(autotune, "_time_sample", fake_time)
+    monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
+    lens = np.array([100] * 20 + [150] * 20 + [1000] * 20)
+    pairs = synth.all_pairs(len(lens))
+    ctx = FakeCtx()
+    choice, timings = autotune.tune(ctx, lens, pairs, gpu_name="fake", target_cells=1e9)
+    assert choice == (16, 16, 192) and ctx.get_tuning() == choice
+    tiny = [t for t in ctx.timed if t[2] == 128]
+    assert len(tiny) == len(autotune.CANDIDATES)
+    # 0 and 64 split the sample the same way (no first sequence is that short): one of them is timed
+    assert sum(1 for t in ctx.timed if t[2] in (0, 64)) == 1
+    # cached: a second call does not time anything
+    ctx2 = FakeCtx()
+    choice2, timings2 = autotune.tune(ctx2, lens, pairs, gpu_name="fake", target_cells=1e9)
+    assert choice2 == choice and timings2 == {} and ctx2.timed == [] and ctx2.get_tuning() == choice
