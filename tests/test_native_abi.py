@@ -119,3 +119,31 @@ def test_autotune_search_and_cache_cpu(tmp_path, monkeypatch):
     ctx2 = FakeCtx()
     choice2, timings2 = autotune.tune(ctx2, lens, pairs, gpu_name="fake", target_cells=1e9)
     assert choice2 == choice and timings2 == {} and ctx2.timed == [] and ctx2.get_tuning() == choice
+
+
+def test_missing_library_fails_loudly(monkeypatch, tmp_path):
+    """No CPU fallback: without the built library the package raises instead
+    of computing anything."""
+    from clustalw_gb300 import _build, native
+
+    monkeypatch.setattr(native, "_lib", None)
+    monkeypatch.setattr(_build, "LIB_PATH", str(tmp_path / "absent" / "libcwgpu.so"))
+    with pytest.raises(RuntimeError, match="missing"):
+        native.load(build=False)
+
+
+def test_bench_distmatrix_packing_matches_symmatrix():
+    """bench.py fills the reference's packed SymMatrix from a pair list the
+    way FullPairwiseAlign's SetAt does (float distance stored as double)."""
+    import bench
+    from clustalw_gb300 import synth
+    from clustalw_gb300.pairwise import DistMatrix
+
+    n = 7
+    pairs = synth.all_pairs(n)
+    dist = np.linspace(0.05, 0.95, len(pairs)).astype(np.float32)
+    el = bench.packed_distmatrix(n, pairs, dist)
+    dm = DistMatrix(n + 1)
+    for (i, j), d in zip(pairs, dist):
+        dm.SetAt(int(i) + 1, int(j) + 1, float(np.float64(d)))
+    assert np.array_equal(el, dm.getElements())
