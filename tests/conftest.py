@@ -46,9 +46,30 @@ def load_golden(name):
 
 def golden_names():
     """Full-pairwise fixtures (guide-tree fixtures start with nj_, quick
-    k-tuple fixtures with fast_)."""
+    k-tuple fixtures with fast_, compact full-size ones with big_)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_")))
+                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_", "big_")))
+
+
+def big_golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("big_") and f.endswith(".npz"))
+
+
+def load_big_golden(name):
+    """A compact fixture written by tests/golden/make_big_golden.py: the
+    reference's 1000-sequence test set, the SHA-256 of the DistMatrix the
+    reference filled and a sample of its entries."""
+    z = np.load(os.path.join(GOLDEN, name + ".npz"))
+    lens = z["lens"]
+    offs = np.concatenate([[0], np.cumsum(lens)[:-1]]).astype(np.int64)
+    seqs = [z["codes"][o : o + L].astype(np.int8) for o, L in zip(offs, lens)]
+    pi, pf = z["params_int"], z["params_float"]
+    params = dict(dna=int(pi[0]), int_scale=int(pi[1]), mat_avg=int(pi[2]), gap_pos1=int(pi[3]),
+                  gap_pos2=int(pi[4]), pw_gap_open=float(pf[0]), pw_gap_extend=float(pf[1]),
+                  gap_open_scale=float(pf[2]), gap_extend_scale=float(pf[3]))
+    return dict(name=name, seqs=seqs, matrix=z["matrix"], params=params, range=tuple(int(x) for x in z["range"]),
+                sha256=bytes(z["elements_sha256"]), n_elements=int(z["n_elements"]),
+                sample_idx=z["sample_idx"], sample_val=z["sample_val"])
 
 
 FAST_KEYS = ("dna", "ktup", "window", "window_gap", "signif", "percent", "max_aa", "max_aln_length")

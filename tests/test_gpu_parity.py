@@ -5,7 +5,7 @@ Myers-Miller score, identity and match counts)."""
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, range_pairs, sym_index
+from conftest import big_golden_names, golden_names, load_big_golden, load_golden, range_pairs, sym_index
 
 pytestmark = pytest.mark.gpu
 
@@ -227,3 +227,19 @@ def test_short_pair_kernel_dna(ctx, oracle_mod):
     assert np.array_equal(dist, want["dist"])
     for f in STAT_FIELDS:
         assert np.array_equal(st[f], want[f]), f
+
+
+@pytest.mark.parametrize("name", big_golden_names())
+def test_full_size_reference_fixture(ctx, name):
+    """The reference's own 1000-sequence test sets (test_data/correct), the
+    whole DistMatrix through the drop-in range call: its SHA-256 equals that
+    of the matrix the unmodified reference filled, and so do sampled entries."""
+    import hashlib
+
+    g = load_big_golden(name)
+    setup(ctx, g)
+    n = len(g["seqs"])
+    elements = np.zeros(g["n_elements"])
+    ctx.pairwise_align(*g["range"], elements, n + 1)
+    assert np.array_equal(elements[g["sample_idx"]].view(np.int64), g["sample_val"].view(np.int64))
+    assert hashlib.sha256(np.ascontiguousarray(elements, dtype="<f8").tobytes()).digest() == g["sha256"]

@@ -4,7 +4,7 @@ edge cases (tests/golden/). Bit-exact: the reference stores a float in a double.
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_golden, range_pairs, sym_index
+from conftest import golden_names, load_big_golden, load_golden, range_pairs, sym_index
 
 
 @pytest.mark.parametrize("name", golden_names())
@@ -27,3 +27,20 @@ def test_gap_penalties_match_reference_types(oracle_mod):
     assert oracle_mod.gap_penalties(prot, 97, 96)[1] == 1
     assert oracle_mod.gap_penalties(prot, 97, 97)[0] == 2390
     assert oracle_mod.gap_penalties(prot, 1523, 1600)[0] == 2841
+
+
+def test_oracle_matches_reference_on_1000_97(oracle_mod):
+    """The oracle on the reference's own 1000 x 97 test set, all 499,500
+    pairs: the DistMatrix it fills hashes to what the unmodified reference
+    filled (the larger compact fixtures are checked on the GPU only)."""
+    import hashlib
+
+    g = load_big_golden("big_1000_97")
+    n = len(g["seqs"])
+    pairs = range_pairs(n, *g["range"])
+    r = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    el = np.zeros(g["n_elements"])
+    si, sj = pairs[:, 0].astype(np.int64), pairs[:, 1].astype(np.int64)
+    el[(sj * (sj + 1)) // 2 + si] = r["dist"].astype(np.float64)
+    assert np.array_equal(el[g["sample_idx"]].view(np.int64), g["sample_val"].view(np.int64))
+    assert hashlib.sha256(np.ascontiguousarray(el, dtype="<f8").tobytes()).digest() == g["sha256"]
