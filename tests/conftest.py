@@ -52,7 +52,20 @@ def golden_names():
 
 
 def big_golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("big_") and f.endswith(".npz"))
+    return sorted(f[:-4] for f in os.listdir(GOLDEN)
+                  if f.startswith("big_") and not f.startswith("big_extra_") and f.endswith(".npz"))
+
+
+def load_big_extra(name):
+    """Tree and quick-distance hashes for a compact full-size fixture
+    (tests/golden/make_big_golden.py --extras); None if not generated."""
+    path = os.path.join(GOLDEN, name.replace("big_", "big_extra_", 1) + ".npz")
+    if not os.path.exists(path):
+        return None
+    z = np.load(path)
+    return dict(nj_sha256=bytes(z["nj_sha256"]), fast_sha256=bytes(z["fast_sha256"]),
+                fast_params=dict(zip(FAST_KEYS, (int(v) for v in z["fast_params"]))),
+                fast_sample_idx=z["fast_sample_idx"], fast_sample_val=z["fast_sample_val"])
 
 
 def load_big_golden(name):

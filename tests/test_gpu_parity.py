@@ -5,7 +5,7 @@ Myers-Miller score, identity and match counts)."""
 import numpy as np
 import pytest
 
-from conftest import big_golden_names, golden_names, load_big_golden, load_golden, range_pairs, sym_index
+from conftest import big_golden_names, golden_names, load_big_extra, load_big_golden, load_golden, range_pairs, sym_index
 
 pytestmark = pytest.mark.gpu
 
@@ -233,7 +233,9 @@ def test_short_pair_kernel_dna(ctx, oracle_mod):
 def test_full_size_reference_fixture(ctx, name):
     """The reference's own 1000-sequence test sets (test_data/correct), the
     whole DistMatrix through the drop-in range call: its SHA-256 equals that
-    of the matrix the unmodified reference filled, and so do sampled entries."""
+    of the matrix the unmodified reference filled, and so do sampled entries.
+    Then the guide tree on it and the quick k-tuple distances of the same
+    set, each against what the unmodified NJTree / FastPairwiseAlign leave."""
     import hashlib
 
     g = load_big_golden(name)
@@ -243,3 +245,21 @@ def test_full_size_reference_fixture(ctx, name):
     ctx.pairwise_align(*g["range"], elements, n + 1)
     assert np.array_equal(elements[g["sample_idx"]].view(np.int64), g["sample_val"].view(np.int64))
     assert hashlib.sha256(np.ascontiguousarray(elements, dtype="<f8").tobytes()).digest() == g["sha256"]
+    x = load_big_extra(name)
+    if x is None:
+        return
+    # The guide tree on that matrix, as the reference's NJTree leaves it.
+    from clustalw_gb300.tree import NJGpu
+
+    nj = NJGpu(0)
+    left, right, desc, _ = nj.tree(n, elements)
+    nj.close()
+    h = hashlib.sha256()
+    for a in (left.astype("<f8"), right.astype("<f8"), desc.astype("<i4"), elements.astype("<f8")):
+        h.update(np.ascontiguousarray(a).tobytes())
+    assert h.digest() == x["nj_sha256"]
+    # The quick k-tuple distances of the same sequences, as FastPairwiseAlign fills them.
+    quick = np.zeros(g["n_elements"])
+    ctx.fast_pairwise_align(x["fast_params"], *g["range"], quick, n + 1)
+    assert np.array_equal(quick[x["fast_sample_idx"]].view(np.int64), x["fast_sample_val"].view(np.int64))
+    assert hashlib.sha256(np.ascontiguousarray(quick, dtype="<f8").tobytes()).digest() == x["fast_sha256"]
