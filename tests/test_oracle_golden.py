@@ -44,3 +44,19 @@ def test_oracle_matches_reference_on_1000_97(oracle_mod):
     el[(sj * (sj + 1)) // 2 + si] = r["dist"].astype(np.float64)
     assert np.array_equal(el[g["sample_idx"]].view(np.int64), g["sample_val"].view(np.int64))
     assert hashlib.sha256(np.ascontiguousarray(el, dtype="<f8").tobytes()).digest() == g["sha256"]
+
+
+@pytest.mark.parametrize("name", ["big_1000_498", "big_1000_1002", "big_1000_1523"])
+def test_oracle_matches_reference_samples_full_size(oracle_mod, name):
+    """The oracle on the 2,000 sampled pairs of the reference's larger
+    1000-sequence sets (protein 498, DNA 1002 and 1523): each distance equals
+    the entry the unmodified reference wrote."""
+    g = load_big_golden(name)
+    idx = g["sample_idx"].astype(np.int64)
+    sj = ((np.sqrt(8 * idx.astype(np.float64) + 1) - 1) // 2).astype(np.int64)
+    sj += (sj + 1) * (sj + 2) // 2 <= idx  # guard the float square root at exact boundaries
+    si = idx - sj * (sj + 1) // 2
+    assert np.all((si >= 0) & (si < sj))
+    pairs = np.stack([si, sj], axis=1).astype(np.int32)
+    r = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    assert np.array_equal(r["dist"].astype(np.float64).view(np.int64), g["sample_val"].view(np.int64))
