@@ -4,8 +4,8 @@
  * (CPU/clustalw-2.0.11/src/pairwise/FullPairwiseAlign.cpp:34-660).
  *
  * TEST INFRASTRUCTURE ONLY. Only tests/, __graft_entry__.smoke() and bench.py's
- * CPU-baseline leg load this library, and only as the checker or the timed CPU
- * baseline. The GPU library never links or calls it.
+ * CPU-baseline leg load this library, and only to check the GPU results or as
+ * the timed CPU baseline. The GPU library never links or calls it.
  *
  * Parity is pinned: tests/test_oracle_golden.py checks this restatement
  * against distance matrices written by the unmodified reference

@@ -1,8 +1,8 @@
 """ctypes wrapper of the oracle restatement (oracle/oracle.c) and a reader for
 the reference harness output (oracle/ref_harness.cpp).
 
-TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() as
-the checker and by bench.py's CPU-baseline leg. The product never imports it.
+TEST INFRASTRUCTURE ONLY: imported by tests/, by __graft_entry__.smoke() to
+check the GPU results and by bench.py's CPU-baseline leg. The product never imports it.
 """
 import ctypes
 import os
