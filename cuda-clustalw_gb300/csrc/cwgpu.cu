@@ -25,6 +25,7 @@
 #include "cwgpu.h"
 #include "cwgpu_context.h"
 #include "cwgpu_device.cuh"
+#include "cwgpu_ranges.h"
 
 namespace {
 
@@ -260,6 +261,8 @@ int check_ready(cwgpu_context* ctx) {
 
 int validate_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs) {
     if (npairs < 0 || (npairs > 0 && !pairs)) return fail(ctx, CWGPU_ERR_ARG, "bad pair list");
+    if (npairs > CWGPU_MAX_PAIRS_PER_CALL)
+        return fail(ctx, CWGPU_ERR_ARG, "more than CWGPU_MAX_PAIRS_PER_CALL pairs in one call");
     for (int64_t q = 0; q < npairs; ++q) {
         const int32_t a = pairs[2 * q], b = pairs[2 * q + 1];
         if (a < 0 || a >= ctx->nseqs || b < 0 || b >= ctx->nseqs)
@@ -404,9 +407,9 @@ int cwgpu_gap_penalties(const cwgpu_params* p, int32_t n, int32_t m, int32_t* ga
 
 int64_t cwgpu_range_pair_count(int32_t nseqs, int32_t i_start, int32_t i_end, int32_t j_start, int32_t j_end) {
     int64_t c = 0;
+    const int64_t hi = std::min(nseqs, j_end);
     for (int32_t si = std::max(0, i_start); si < nseqs && si < i_end; ++si) {
-        const int32_t lo = std::max(si + 1, j_start + 1);
-        const int32_t hi = std::min(nseqs, j_end);
+        const int64_t lo = cwgpu::range_col_lo(si, j_start);
         if (hi > lo) c += hi - lo;
     }
     return c;
@@ -760,22 +763,19 @@ int cwgpu_pairwise_align(cwgpu_context* ctx, int32_t i_start, int32_t i_end, int
         return fail(ctx, CWGPU_ERR_RANGE, "The range for pairwise Alignment is incorrect.");
     const int n = ctx->nseqs;
     if (n == 0) return CWGPU_OK;  // :63-66
-    std::vector<int32_t> pairs;
-    for (int32_t si = std::max(0, i_start); si < n && si < i_end; ++si)
-        for (int32_t sj = std::max(si + 1, j_start + 1); sj < n && sj < j_end; ++sj) {
-            pairs.push_back(si);
-            pairs.push_back(sj);
-        }
-    const int64_t np = (int64_t)pairs.size() / 2;
-    std::vector<float> dist((size_t)std::max<int64_t>(np, 1));
-    int rc = cwgpu_align_pairs(ctx, pairs.data(), np, dist.data(), stats_out);
-    if (rc) return rc;
-    for (int64_t q = 0; q < np; ++q) {
-        // SymMatrix::getIndex for (si+1, sj+1), si < sj: ((_j*(_j+1))>>1) + _i.
-        const int64_t i = pairs[2 * q], j = pairs[2 * q + 1];
-        elements[((j * (j + 1)) >> 1) + i] = (double)dist[q];
-    }
-    return CWGPU_OK;
+    std::vector<float> dist;
+    return cwgpu::for_range_blocks(
+        n, i_start, i_end, j_start, j_end, cwgpu::kRangeBlockPairs, [&](const int32_t* pairs, int64_t np, int64_t first) {
+            dist.resize((size_t)std::max<int64_t>(np, 1));
+            const int rc = cwgpu_align_pairs(ctx, pairs, np, dist.data(), stats_out ? stats_out + first : nullptr);
+            if (rc) return rc;
+            for (int64_t q = 0; q < np; ++q) {
+                // SymMatrix::getIndex for (si+1, sj+1), si < sj: ((_j*(_j+1))>>1) + _i.
+                const int64_t i = pairs[2 * q], j = pairs[2 * q + 1];
+                elements[((j * (j + 1)) >> 1) + i] = (double)dist[q];
+            }
+            return (int)CWGPU_OK;
+        });
 }
 
 int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning) {

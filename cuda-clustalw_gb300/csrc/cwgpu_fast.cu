@@ -43,6 +43,7 @@
 
 #include "cwgpu.h"
 #include "cwgpu_context.h"
+#include "cwgpu_ranges.h"
 
 namespace cwfast {
 
@@ -812,6 +813,8 @@ extern "C" {
 int cwgpu_fast_align_pairs(cwgpu_context* ctx, const cwgpu_fast_params* p, const int32_t* pairs, int64_t npairs,
                            double* dist_out, cwgpu_fast_stats* stats_out) {
     if (!ctx || npairs < 0 || (npairs > 0 && (!pairs || !dist_out))) return CWGPU_ERR_ARG;
+    if (npairs > CWGPU_MAX_PAIRS_PER_CALL)
+        return ffail(ctx, CWGPU_ERR_ARG, "more than CWGPU_MAX_PAIRS_PER_CALL pairs in one call");
     if (!ctx->has_seqs) return ffail(ctx, CWGPU_ERR_STATE, "sequences not set");
     Params P;
     int rc = make_params(ctx, p, &P);
@@ -878,6 +881,8 @@ int cwgpu_fast_align_pairs_device(cwgpu_context* ctx, const cwgpu_fast_params* p
                                   const int32_t* d_order, int64_t npairs, double* d_dist,
                                   cwgpu_fast_stats* d_stats, void* stream) {
     if (!ctx || npairs < 0 || (npairs > 0 && (!d_pairs || !d_dist))) return CWGPU_ERR_ARG;
+    if (npairs > CWGPU_MAX_PAIRS_PER_CALL)
+        return ffail(ctx, CWGPU_ERR_ARG, "more than CWGPU_MAX_PAIRS_PER_CALL pairs in one call");
     if (!ctx->has_seqs) return ffail(ctx, CWGPU_ERR_STATE, "sequences not set");
     Params P;
     int rc = make_params(ctx, p, &P);
@@ -898,22 +903,20 @@ int cwgpu_fast_pairwise_align(cwgpu_context* ctx, const cwgpu_fast_params* p, in
         return ffail(ctx, CWGPU_ERR_RANGE, "The range for pairwise Alignment is incorrect.");
     // FastPairwiseAlign.cpp:65-84: i = iStart+1..iEnd, j = max(jStart+2, i+1)..jEnd
     // (1-based), i.e. si in [iStart, iEnd), sj in [max(jStart+1, si+1), jEnd),
-    // held inside the sequence set.
-    std::vector<int32_t> pairs;
-    for (int si = i_start; si < std::min(n, i_end); ++si)
-        for (int sj = std::max(j_start + 1, si + 1); sj < std::min(n, j_end); ++sj) {
-            pairs.push_back(si);
-            pairs.push_back(sj);
-        }
-    const int64_t np = (int64_t)pairs.size() / 2;
-    std::vector<double> dist(std::max<int64_t>(np, 1));
-    int rc = cwgpu_fast_align_pairs(ctx, p, pairs.data(), np, dist.data(), stats_out);
-    if (rc) return rc;
-    for (int64_t q = 0; q < np; ++q) {
-        const int64_t a = pairs[2 * q + 1], b = pairs[2 * q];  // getIndex(si+1, sj+1), si < sj
-        elements[((a * (a + 1)) >> 1) + b] = dist[q];
-    }
-    return CWGPU_OK;
+    // held inside the sequence set; whole rows per call.
+    std::vector<double> dist;
+    return cwgpu::for_range_blocks(
+        n, i_start, i_end, j_start, j_end, cwgpu::kRangeBlockPairs, [&](const int32_t* pairs, int64_t np, int64_t first) {
+            dist.resize((size_t)std::max<int64_t>(np, 1));
+            const int rc =
+                cwgpu_fast_align_pairs(ctx, p, pairs, np, dist.data(), stats_out ? stats_out + first : nullptr);
+            if (rc) return rc;
+            for (int64_t q = 0; q < np; ++q) {
+                const int64_t a = pairs[2 * q + 1], b = pairs[2 * q];  // getIndex(si+1, sj+1), si < sj
+                elements[((a * (a + 1)) >> 1) + b] = dist[q];
+            }
+            return (int)CWGPU_OK;
+        });
 }
 
 }  // extern "C"

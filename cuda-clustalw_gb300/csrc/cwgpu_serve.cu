@@ -652,8 +652,15 @@ int cwgpu_server_submit(cwgpu_server* s, int32_t nseqs, const int8_t* codes, con
         j->lmax = std::max(j->lmax, (int)lens[q]);
     }
     j->npairs = (int64_t)nseqs * (nseqs - 1) / 2;
-    for (int a = 0; a < nseqs; ++a)
-        for (int b = a + 1; b < nseqs; ++b) j->cells_nm += (int64_t)lens[a] * lens[b];
+    if (j->npairs > CWGPU_MAX_PAIRS_PER_CALL) {  // work items carry 32-bit pair indices
+        delete j;
+        return srv_fail(s, CWGPU_ERR_ARG, "job has more than CWGPU_MAX_PAIRS_PER_CALL pairs");
+    }
+    int64_t before = 0;  // residues of the sequences before b
+    for (int b = 0; b < nseqs; ++b) {
+        j->cells_nm += before * lens[b];
+        before += lens[b];
+    }
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->fatal) {
         delete j;

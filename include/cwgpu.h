@@ -34,6 +34,11 @@ extern "C" {
 
 #define CWGPU_NUMRES 32       /* clustalw NUMRES (general/clustalw.h:231) */
 #define CWGPU_MAX_SEQ_LEN 65535 /* longest sequence a context accepts */
+/* Longest pair list one call takes (the work order holds 32-bit positions).
+ * The range calls (cwgpu_pairwise_align, cwgpu_fast_pairwise_align) split
+ * larger ranges into blocks of whole rows themselves; a served job may have at
+ * most this many pairs. */
+#define CWGPU_MAX_PAIRS_PER_CALL 2147483647LL
 
 typedef enum cwgpu_status {
     CWGPU_OK = 0,

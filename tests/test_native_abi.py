@@ -59,6 +59,10 @@ def test_range_pair_count(lib):
 
     for rng in [(0, 10, 0, 10), (0, 10, 4, 10), (3, 7, 0, 10), (5, 5, 0, 10), (0, 100, 0, 100), (8, 20, 9, 30)]:
         assert native.range_pair_count(10, *rng) == len(range_pairs(10, *rng))
+    big = 2**31 - 1  # column start at INT32_MAX selects no column (no 32-bit wrap)
+    assert native.range_pair_count(10, 0, 10, big, big) == 0
+    assert native.range_pair_count(10, 0, big, 0, big) == 45
+    assert native.range_pair_count(70000, 0, 70000, 0, 70000) == 70000 * 69999 // 2
 
 
 def test_status_strings(lib):
