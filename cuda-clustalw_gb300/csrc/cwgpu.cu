@@ -688,11 +688,11 @@ int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
         CW_CUDA(ctx, grow(ctx->d_stats1, c4, npairs));
         ctx->cap_pairs1 = npairs;
     }
-    if (!ctx->stream_short) {
-        CW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream_short, cudaStreamNonBlocking));
-        CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
-        CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
-    }
+    // Created on first use; each handle on its own, so a call after a failed
+    // creation retries what is missing.
+    if (!ctx->stream_short) CW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream_short, cudaStreamNonBlocking));
+    if (!ctx->ev_fork) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
+    if (!ctx->ev_join) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
     int64_t nlong = 0;
     const std::vector<int32_t> order = work_order(ctx, pairs, npairs, &nlong);
     cudaStream_t s = ctx->stream;
