@@ -229,6 +229,51 @@ def test_short_pair_kernel_dna(ctx, oracle_mod):
         assert np.array_equal(st[f], want[f]), f
 
 
+def test_maximum_length_sequences(oracle_mod):
+    """Sequences at the length limit (CWGPU_MAX_SEQ_LEN = 65,535 residues): a
+    300-residue fragment (long-pair kernel) and a 99-residue one (short-pair
+    kernel) against the full-length sequence in both orders, and a pair of
+    about 16,000 residues whose Myers-Miller stage recurses 14 levels deep;
+    every distance and intermediate equals the oracle's. One residue more is
+    rejected at upload. A context of its own: its scratch rows are sized for
+    65,536 columns."""
+    from clustalw_gb300 import load_matrix, native, synth
+
+    rng = np.random.default_rng(65535)
+
+    def rand(length):
+        pick = rng.choice(len(synth.PROTEIN_CODES), size=length, p=synth.PROTEIN_PROBS)
+        return synth.PROTEIN_CODES[pick].astype(np.int8)
+
+    def mutate(seq, rate):
+        seq = seq.copy()
+        hit = rng.random(len(seq)) < rate
+        seq[hit] = rand(int(hit.sum()))
+        return seq[rng.random(len(seq)) >= 0.01]  # and delete about 1 % of the residues
+
+    full = rand(65535)
+    seqs = [full, mutate(full[30000:30300], 0.2), full[:16384].copy(), mutate(full[:16384], 0.2),
+            mutate(full[100:200], 0.2)]
+    assert len(seqs[4]) <= 128 < len(seqs[1])
+    matrix, params = load_matrix("protein")
+    c = native.Context(0)
+    try:
+        c.set_matrix(matrix)
+        c.set_params(params)
+        with pytest.raises(native.CwgpuError):
+            c.upload_seqs([rand(65536)])
+        c.upload_seqs(seqs)
+        pairs = np.array([[0, 1], [1, 0], [4, 0], [0, 4], [2, 3], [3, 2]], dtype=np.int32)
+        dist, st = c.align_pairs(pairs, stats=True)
+    finally:
+        c.close()
+    want = oracle_mod.align_pairs(seqs, matrix, params, pairs)
+    assert np.array_equal(dist, want["dist"])
+    for f in STAT_FIELDS:
+        assert np.array_equal(st[f], want[f]), f
+    assert want["se1"][4] - want["sb1"][4] > 8192  # the deep Myers-Miller box
+
+
 @pytest.mark.parametrize("name", big_golden_names())
 def test_full_size_reference_fixture(ctx, name):
     """The reference's own 1000-sequence test sets (test_data/correct), the
