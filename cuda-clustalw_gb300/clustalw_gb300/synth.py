@@ -117,6 +117,29 @@ def uneven_protein(nfamilies=8, per_family=125, lo=30, hi=2000, seed=0):
     return seqs
 
 
+def length_limit_set(max_len=65535, seed=65535):
+    """Sequences at the length limit: a max_len-residue random protein, a
+    300-residue and a 100-residue fragment of it (20 % of the sites
+    substituted, then about 1 % deleted), a 16,384-residue prefix of it and a
+    mutated copy of that prefix (a pair whose Myers-Miller stage recurses 14
+    levels)."""
+    rng = np.random.default_rng(seed)
+
+    def rand(length):
+        pick = rng.choice(len(PROTEIN_CODES), size=length, p=PROTEIN_PROBS)
+        return PROTEIN_CODES[pick].astype(np.int8)
+
+    def mutate(seq, rate):
+        seq = seq.copy()
+        hit = rng.random(len(seq)) < rate
+        seq[hit] = rand(int(hit.sum()))
+        return seq[rng.random(len(seq)) >= 0.01]
+
+    full = rand(max_len)
+    return [full, mutate(full[30000:30300], 0.2), full[:16384].copy(), mutate(full[:16384], 0.2),
+            mutate(full[100:200], 0.2)]
+
+
 # The benchmark workloads (sizes as the reference's headline measurements use them).
 WORKLOADS = {
     "protein-100x97": lambda seed=0: protein_family(100, 97, seed),

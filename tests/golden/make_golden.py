@@ -4,6 +4,8 @@ through oracle/_ref/refharness.
 
 Run from the repository root, where the reference tree is available:
     python tests/golden/make_golden.py
+(--nj-only, --fast-only or --limits writes only the guide-tree, quick-distance
+or length-limit fixtures.)
 
 Each <name>.npz holds the encoded sequences exactly as the reference's reader
 produced them, the pairwise matrix and scalars the reference used, the range,
@@ -146,6 +148,15 @@ def make_nj():
     save_nj("nj_ties_30", n, el)
 
 
+def make_limits():
+    """Sequences at the length limit (synth.length_limit_set): the 65,535-residue
+    sequence with its 300- and 100-residue fragments, and the 16,384-residue
+    pair whose Myers-Miller stage recurses 14 levels."""
+    seqs = synth.length_limit_set()
+    save("limit_65535", run_fasta(synth.to_fasta([seqs[0], seqs[1], seqs[4]]), "m"))
+    save("limit_deep_16384", run_fasta(synth.to_fasta([seqs[2], seqs[3]]), "q"))
+
+
 def main():
     O.build()
     mats = {}
@@ -195,6 +206,7 @@ def main():
     text = "".join(f">e{i}\n{s}\n" for i, s in enumerate(edge))
     save("edge_protein", run_fasta(text, "e"))
 
+    make_limits()
     make_nj()
     make_fast()
 
@@ -211,5 +223,8 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--fast-only":
         O.build()
         make_fast()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--limits":
+        O.build()
+        make_limits()
     else:
         main()

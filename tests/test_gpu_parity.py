@@ -239,29 +239,15 @@ def test_maximum_length_sequences(oracle_mod):
     65,536 columns."""
     from clustalw_gb300 import load_matrix, native, synth
 
-    rng = np.random.default_rng(65535)
-
-    def rand(length):
-        pick = rng.choice(len(synth.PROTEIN_CODES), size=length, p=synth.PROTEIN_PROBS)
-        return synth.PROTEIN_CODES[pick].astype(np.int8)
-
-    def mutate(seq, rate):
-        seq = seq.copy()
-        hit = rng.random(len(seq)) < rate
-        seq[hit] = rand(int(hit.sum()))
-        return seq[rng.random(len(seq)) >= 0.01]  # and delete about 1 % of the residues
-
-    full = rand(65535)
-    seqs = [full, mutate(full[30000:30300], 0.2), full[:16384].copy(), mutate(full[:16384], 0.2),
-            mutate(full[100:200], 0.2)]
-    assert len(seqs[4]) <= 128 < len(seqs[1])
+    seqs = synth.length_limit_set()
+    assert len(seqs[0]) == 65535 and len(seqs[4]) <= 128 < len(seqs[1])
     matrix, params = load_matrix("protein")
     c = native.Context(0)
     try:
         c.set_matrix(matrix)
         c.set_params(params)
         with pytest.raises(native.CwgpuError):
-            c.upload_seqs([rand(65536)])
+            c.upload_seqs([np.resize(seqs[0], 65536)])
         c.upload_seqs(seqs)
         pairs = np.array([[0, 1], [1, 0], [4, 0], [0, 4], [2, 3], [3, 2]], dtype=np.int32)
         dist, st = c.align_pairs(pairs, stats=True)
