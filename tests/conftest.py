@@ -92,6 +92,11 @@ def fast_golden_names():
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("fast_") and f.endswith(".npz"))
 
 
+def quick_limit_names():
+    """Quick-distance fixtures at the quick path's 8191-residue limit."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("quicklimit_") and f.endswith(".npz"))
+
+
 def load_fast_golden(name):
     """A quick-distance fixture: FastPairwiseAlign::pairwiseAlign of the reference
     (pairwise/FastPairwiseAlign.cpp:20-139) on the stored sequences."""

@@ -157,6 +157,30 @@ def make_limits():
     save("limit_deep_16384", run_fasta(synth.to_fasta([seqs[2], seqs[3]]), "q"))
 
 
+def make_quick_limits():
+    """Quick distances at the quick path's length limit (8191 residues):
+    protein (ktup 1) and DNA (ktup 2) sets of an 8191-residue sequence, a
+    mutated copy of it and a fragment. Named quicklimit_*: only the oracle
+    test reads them."""
+    rng = np.random.default_rng(8191)
+
+    def mutate(seq, rate, codes):
+        seq = seq.copy()
+        hit = rng.random(len(seq)) < rate
+        seq[hit] = codes[rng.integers(0, len(codes), int(hit.sum()))]
+        return seq[rng.random(len(seq)) >= 0.01]
+
+    for tag, codes, probs in (("protein", synth.PROTEIN_CODES, synth.PROTEIN_PROBS),
+                              ("dna", synth.DNA_CODES, synth.DNA_PROBS)):
+        full = codes[rng.choice(len(codes), size=8191, p=probs)].astype(np.int8)
+        seqs = [full, mutate(full, 0.15, codes), mutate(full[2000:2600], 0.1, codes)]
+        with tempfile.TemporaryDirectory() as d:
+            fa = os.path.join(d, "s.fa")
+            with open(fa, "w") as f:
+                f.write(synth.to_fasta(seqs))
+            save_fast("quicklimit_" + tag + "_8191", O.run_reference(fa, os.path.join(d, "o.bin"), fast=True))
+
+
 def main():
     O.build()
     mats = {}
@@ -209,6 +233,7 @@ def main():
     make_limits()
     make_nj()
     make_fast()
+    make_quick_limits()
 
     os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
     with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
@@ -226,5 +251,6 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--limits":
         O.build()
         make_limits()
+        make_quick_limits()
     else:
         main()
