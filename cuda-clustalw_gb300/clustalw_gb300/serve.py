@@ -143,16 +143,17 @@ def run_arrivals(server, jobs, rate, seed=0):
                 break
             done_any = False
             for k in sorted(pending):
-                if server.poll(ids[k]) in (JOB_DONE, JOB_FAILED):
-                    try:
-                        _, _, times = server.result(ids[k])
-                        records[k] = times
-                        server.release(ids[k])
-                    except CwgpuError as e:  # surfaced after the run
-                        errors.append(e)
-                        records[k] = np.array([np.nan] * 4)
-                    pending.discard(k)
-                    done_any = True
+                try:
+                    if server.poll(ids[k]) not in (JOB_DONE, JOB_FAILED):
+                        continue
+                    _, _, times = server.result(ids[k])
+                    records[k] = times
+                    server.release(ids[k])
+                except CwgpuError as e:  # surfaced after the run
+                    errors.append(e)
+                    records[k] = np.array([np.nan] * 4)
+                pending.discard(k)
+                done_any = True
             if not done_any:
                 time.sleep(0.001)
 
