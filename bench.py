@@ -581,7 +581,12 @@ def ours_arm(args):
     if not np.array_equal(dist_out, ref_dist):
         raise RuntimeError("distances changed between runs")
     ms = 1e3 * total_s / args.steps
-    value = world * cells_nm * args.steps / total_s / 1e9
+    cells_all = cells_nm  # every rank's replica has its own seed: sum the ranks' cells
+    if world > 1:
+        c = torch.tensor([float(cells_nm)], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(c)
+        cells_all = float(c.item())
+    value = cells_all * args.steps / total_s / 1e9
     if args.device_only:
         if rank == 0:
             print(json.dumps({"metric": "GCUPS", "value": value, "ms_per_step": ms, "pairs": int(len(pairs)),
@@ -602,6 +607,10 @@ def ours_arm(args):
         if k == 0 and not np.array_equal(d, ref_dist):
             raise RuntimeError("e2e distances differ from the device-resident run")
     e2e_s = statistics.mean(e2e_times[1:])
+    if world > 1:  # the slowest rank's call, like the device-resident number
+        t = torch.tensor([e2e_s], device="cuda", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
     lmax = int(packed[2].max()) if len(packed[2]) else 0
     codes_padded = int(sum((int(L) + 15) & ~15 for L in packed[2]))
     h2d = codes_padded + 8 * len(seqs) + 4 * len(seqs) + 4 * len(seqs) + 4 * (lmax + 1) + 4 * 1024
@@ -668,7 +677,7 @@ def ours_arm(args):
             "tuning": tuning,
         },
         "e2e": {
-            "value": cells_nm / e2e_s / 1e9,
+            "value": cells_all / e2e_s / 1e9,
             "unit": "GCUPS",
             "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h,
