@@ -10,7 +10,9 @@ ones mostly large), so the tuner times a length-stratified sample of the
 workload's pairs: first each tiny-frame candidate, then each short-pair
 threshold with the chosen tiny-frame pair, and keeps the fastest. Results never
 depend on the knobs, only the time does. Choices are cached per GPU and length
-profile in $XDG_CACHE_HOME/clustalw_gb300/tuning.json.
+profile in $XDG_CACHE_HOME/clustalw_gb300/tuning.json. $CLUSTALW_GB300_TUNING
+("tiny_m,tiny_n,short_rows") overrides both the cache and the search, and is
+applied to every new native.Context.
 """
 import json
 import os
@@ -20,6 +22,20 @@ import numpy as np
 
 CANDIDATES = [(0, 0), (16, 8), (16, 16), (32, 12), (32, 16), (64, 16)]
 SHORT_ROWS = [0, 64, 128, 192, 256]
+ENV_VAR = "CLUSTALW_GB300_TUNING"
+
+
+def env_override():
+    """(tiny_m, tiny_n, short_rows) from $CLUSTALW_GB300_TUNING, e.g. "32,16,128";
+    None when it is unset or empty. A malformed value raises ValueError (the
+    library itself rejects values outside its ranges)."""
+    text = os.environ.get(ENV_VAR, "").strip()
+    if not text:
+        return None
+    parts = [p.strip() for p in text.split(",")]
+    if len(parts) != 3:
+        raise ValueError(f"{ENV_VAR} must be 'tiny_m,tiny_n,short_rows', got {text!r}")
+    return tuple(int(p) for p in parts)
 
 
 def _cache_path():
@@ -72,6 +88,10 @@ def tune(ctx, lens, pairs, gpu_name="gpu", target_cells=2e10, candidates=CANDIDA
     """Pick (tiny_m, tiny_n, short_rows) for this workload on `ctx` (a
     native.Context with matrix, params and sequences set), apply it and return
     (choice, {candidate: seconds})."""
+    forced = env_override()
+    if forced is not None:
+        ctx.set_tuning(*forced)
+        return forced, {}
     key = f"{gpu_name}|{length_profile(lens)}"
     path = _cache_path()
     cache = {}

@@ -252,6 +252,11 @@ class Context:
             raise CwgpuError(rc, "cwgpu_create")
         self._h = h
         self.nseqs = 0
+        from .autotune import env_override  # the knobs' environment override, if set
+
+        forced = env_override()
+        if forced is not None:
+            self.set_tuning(*forced)
 
     def close(self):
         if getattr(self, "_h", None):

@@ -84,6 +84,38 @@ def test_autotune_helpers_cpu():
     assert autotune.length_profile([1523] * 10) != autotune.length_profile([97] * 10)
 
 
+def test_autotune_environment_override(tmp_path, monkeypatch):
+    """$CLUSTALW_GB300_TUNING beats the cache and the search; unset or empty
+    means no override; a malformed value is an error."""
+    from clustalw_gb300 import autotune, synth
+
+    class FakeCtx:
+        t = (32, 16, 128)
+
+        def set_tuning(self, m, n, r=None):
+            self.t = (m, n, r)
+
+        def get_tuning(self):
+            return self.t
+
+    monkeypatch.setattr(autotune, "_time_sample", lambda *a: pytest.fail("timed despite the override"))
+    monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
+    monkeypatch.delenv(autotune.ENV_VAR, raising=False)
+    assert autotune.env_override() is None
+    monkeypatch.setenv(autotune.ENV_VAR, " ")
+    assert autotune.env_override() is None
+    monkeypatch.setenv(autotune.ENV_VAR, "16, 8,256")
+    assert autotune.env_override() == (16, 8, 256)
+    ctx = FakeCtx()
+    lens = np.array([100] * 10)
+    assert autotune.tune(ctx, lens, synth.all_pairs(10), gpu_name="fake") == ((16, 8, 256), {})
+    assert ctx.get_tuning() == (16, 8, 256)
+    for bad in ("16,8", "a,b,c", "1,2,3,4"):
+        monkeypatch.setenv(autotune.ENV_VAR, bad)
+        with pytest.raises(ValueError):
+            autotune.env_override()
+
+
 def test_autotune_search_and_cache_cpu(tmp_path, monkeypatch):
     """The tuner's search on a stand-in context with a known cost model: the
     tiny-frame candidates first, then only the short-pair thresholds that
@@ -110,6 +142,7 @@ def test_autotune_search_and_cache_cpu(tmp_path, monkeypatch):
 
     monkeypatch.setattr(autotune, "_time_sample", fake_time)
     monkeypatch.setenv("XDG_CACHE_HOME", str(tmp_path))
+    monkeypatch.delenv(autotune.ENV_VAR, raising=False)
     lens = np.array([100] * 20 + [150] * 20 + [1000] * 20)
     pairs = synth.all_pairs(len(lens))
     ctx = FakeCtx()
