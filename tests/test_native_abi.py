@@ -116,6 +116,36 @@ def test_autotune_environment_override(tmp_path, monkeypatch):
             autotune.env_override()
 
 
+def test_context_applies_the_tuning_override(monkeypatch):
+    """native.Context sets $CLUSTALW_GB300_TUNING on its new handle, and only
+    when it is set (a stand-in library on the CPU: no device call)."""
+    from clustalw_gb300 import autotune, native
+
+    class FakeLib:
+        def __init__(self):
+            self.tuning = []
+
+        def cwgpu_create(self, device, handle):
+            return 0
+
+        def cwgpu_destroy(self, handle):
+            pass
+
+        def cwgpu_set_tuning(self, handle, ref):
+            t = ref._obj
+            self.tuning.append((t.tiny_m, t.tiny_n, t.short_rows))
+            return 0
+
+    fake = FakeLib()
+    monkeypatch.setattr(native, "load", lambda build=True: fake)
+    monkeypatch.delenv(autotune.ENV_VAR, raising=False)
+    native.Context(0).close()
+    assert fake.tuning == []
+    monkeypatch.setenv(autotune.ENV_VAR, "64,16,192")
+    native.Context(0).close()
+    assert fake.tuning == [(64, 16, 192)]
+
+
 def test_autotune_search_and_cache_cpu(tmp_path, monkeypatch):
     """The tuner's search on a stand-in context with a known cost model: the
     tiny-frame candidates first, then only the short-pair thresholds that
