@@ -46,9 +46,9 @@ def load_golden(name):
 
 def golden_names():
     """Full-pairwise fixtures (guide-tree fixtures start with nj_, quick
-    k-tuple fixtures with fast_, compact full-size ones with big_)."""
+    k-tuple fixtures with fast_ or quicklimit_, compact full-size ones with big_)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_", "big_")))
+                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_", "quicklimit_", "big_")))
 
 
 def big_golden_names():
