@@ -649,6 +649,8 @@ def ours_arm(args):
         "peak_source": f"{props.multi_processor_count} SMs x {INT32_LANES_PER_SM} INT32 lanes x "
         f"{sm_max:.0f} MHz (sm_max_mhz of MEASURED_PEAKS.json)",
         "hbm_peak_gbs": peaks.get("hbm_gbs"),
+        # DRAM bytes per launch over the launch time: how far the kernel is from the HBM roof
+        "hbm_achieved_gbs": (tpc * cells_nm / (ms / 1e3) / 1e9) if tpc is not None else None,
         "traffic_source": tsrc,
     }
 
