@@ -5,7 +5,7 @@ Myers-Miller score, identity and match counts)."""
 import numpy as np
 import pytest
 
-from conftest import big_golden_names, golden_names, load_big_extra, load_big_golden, load_golden, range_pairs, sym_index
+from conftest import big_golden_names, golden_names, load_big_extra, load_big_golden, load_golden, range_pairs
 
 pytestmark = pytest.mark.gpu
 

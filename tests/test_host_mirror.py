@@ -7,7 +7,7 @@ full and partial ranges), with the same per-pair info lines."""
 import numpy as np
 import pytest
 
-from conftest import load_golden, range_pairs, sym_index
+from conftest import load_golden, sym_index
 
 
 def test_symmatrix_index_rule():

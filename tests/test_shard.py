@@ -5,7 +5,6 @@ process would produce. The per-rank compute here is a deterministic stand-in
 import os
 
 import numpy as np
-import pytest
 import torch.distributed as dist
 import torch.multiprocessing as mp
 
