@@ -300,13 +300,17 @@ def read_ref_output(path):
     )
 
 
-def run_reference(fasta, out_bin, rng=None, fast=False):
+def run_reference(fasta, out_bin, rng=None, fast=False, overrides=None):
     """Run the reference harness (needs oracle/_ref/refharness, built here only);
-    fast=True runs FastPairwiseAlign instead of FullPairwiseAlign."""
+    fast=True runs FastPairwiseAlign instead of FullPairwiseAlign. overrides:
+    {"CWREF_PWMATRIX": "blosum"|"pam"|"gonnet"|"id", "CWREF_PWGAPOPEN": "...",
+    "CWREF_PWGAPEXT": "..."}, applied as the reference's -pwmatrix, -pwgapopen
+    and -pwgapext options would be."""
     if not os.path.exists(REF_HARNESS):
         raise FileNotFoundError(REF_HARNESS)
     cmd = [REF_HARNESS] + (["--fast"] if fast else []) + [fasta, out_bin]
     if rng is not None:
         cmd += [str(int(x)) for x in rng]
-    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL)
+    env = dict(os.environ, **overrides) if overrides else None
+    subprocess.run(cmd, check=True, stdout=subprocess.DEVNULL, env=env)
     return read_ref_output(out_bin)

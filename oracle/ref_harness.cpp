@@ -14,6 +14,8 @@
 // Usage: refharness IN.fa OUT.bin [iStart iEnd jStart jEnd]
 //        refharness --fast IN.fa OUT.bin [iStart iEnd jStart jEnd]
 //        refharness --nj IN.dist OUT.tree [OUT.report]
+// (CWREF_PWMATRIX, CWREF_PWGAPOPEN, CWREF_PWGAPEXT in the environment change the
+// pairwise matrix and gap penalties, see apply_overrides.)
 //
 // --fast runs clustalw::FastPairwiseAlign::pairwiseAlign (the k-tuple quick
 // distances, pairwise/FastPairwiseAlign.cpp:20-139) instead; its OUT.bin starts
@@ -72,6 +74,44 @@ static void put(FILE* f, const void* p, size_t n) {
     if (n && fwrite(p, 1, n, f) != n) {
         fprintf(stderr, "refharness: short write\n");
         exit(2);
+    }
+}
+
+// Optional parameter overrides from the environment, set the way clustalw2's
+// -pwmatrix, -pwgapopen and -pwgapext options set them
+// (interface/CommandLineParser.cpp:1811-1850, 2265-2300):
+//   CWREF_PWMATRIX  blosum | pam | gonnet | id   (protein pairwise matrix)
+//   CWREF_PWGAPOPEN, CWREF_PWGAPEXT                (real numbers >= 0)
+// Called after the sequence type is known and before setDNAParams /
+// setProtParams copy the per-type penalties into the pairwise ones.
+static void apply_overrides(bool dna) {
+    const char* m = getenv("CWREF_PWMATRIX");
+    if (m && *m) {
+        const std::string name(m);
+        const int num = name == "blosum" ? 1 : name == "pam" ? 2 : name == "gonnet" ? 3 : name == "id" ? 4 : 0;
+        if (!num) {
+            fprintf(stderr, "refharness: unknown CWREF_PWMATRIX %s\n", m);
+            exit(2);
+        }
+        subMatrix->setCurrentNameAndNum(name, num, Protein, Pairwise);
+    }
+    const char* go = getenv("CWREF_PWGAPOPEN");
+    if (go && *go) {
+        float v = 0.0f;  // sscanf %f like the option parser
+        sscanf(go, "%f", &v);
+        if (dna)
+            userParameters->setDNAPWGapOpenPenalty(v);
+        else
+            userParameters->setProteinPWGapOpenPenalty(v);
+    }
+    const char* ge = getenv("CWREF_PWGAPEXT");
+    if (ge && *ge) {
+        float v = 0.0f;
+        sscanf(ge, "%f", &v);
+        if (dna)
+            userParameters->setDNAPWGapExtendPenalty(v);
+        else
+            userParameters->setProteinPWGapExtendPenalty(v);
     }
 }
 
@@ -145,6 +185,7 @@ int main(int argc, char** argv) {
         fprintf(stderr, "refharness: readSeqs failed with code %d\n", code);
         return 3;
     }
+    apply_overrides(userParameters->getDNAFlag());
     if (userParameters->getDNAFlag())
         userParameters->setDNAParams();
     else

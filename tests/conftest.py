@@ -45,10 +45,17 @@ def load_golden(name):
 
 
 def golden_names():
-    """Full-pairwise fixtures (guide-tree fixtures start with nj_, quick
-    k-tuple fixtures with fast_ or quicklimit_, compact full-size ones with big_)."""
+    """Full-pairwise fixtures with the default parameters (guide-tree fixtures
+    start with nj_, quick k-tuple fixtures with fast_ or quicklimit_, other
+    pairwise parameters with pwparams_, compact full-size ones with big_)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_", "quicklimit_", "big_")))
+                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_", "quicklimit_", "pwparams_", "big_")))
+
+
+def pw_variant_names():
+    """Full-pairwise fixtures under the other protein pairwise matrices (BLOSUM,
+    PAM, identity) and non-default gap penalties (protein and DNA)."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("pwparams_") and f.endswith(".npz"))
 
 
 def big_golden_names():

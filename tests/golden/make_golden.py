@@ -4,8 +4,8 @@ through oracle/_ref/refharness.
 
 Run from the repository root, where the reference tree is available:
     python tests/golden/make_golden.py
-(--nj-only, --fast-only or --limits writes only the guide-tree, quick-distance
-or length-limit fixtures.)
+(--nj-only, --fast-only, --limits or --pw-variants writes only the guide-tree,
+quick-distance, length-limit or pairwise-parameter fixtures.)
 
 Each <name>.npz holds the encoded sequences exactly as the reference's reader
 produced them, the pairwise matrix and scalars the reference used, the range,
@@ -52,12 +52,12 @@ def save(name, ref):
     print(f"{name}: {ref['n']} seqs, range {list(ref['range'])}, ref {ref['seconds']:.2f}s")
 
 
-def run_fasta(text, name, rng=None):
+def run_fasta(text, name, rng=None, overrides=None):
     with tempfile.TemporaryDirectory() as d:
         fa = os.path.join(d, name + ".fa")
         with open(fa, "w") as f:
             f.write(text)
-        return O.run_reference(fa, os.path.join(d, "out.bin"), rng)
+        return O.run_reference(fa, os.path.join(d, "out.bin"), rng, overrides=overrides)
 
 
 def save_fast(name, ref):
@@ -181,6 +181,28 @@ def make_quick_limits():
             save_fast("quicklimit_" + tag + "_8191", O.run_reference(fa, os.path.join(d, "o.bin"), fast=True))
 
 
+PW_VARIANTS = [
+    # (name, protein?, overrides): the other protein pairwise matrices and
+    # non-default gap penalties, as -pwmatrix / -pwgapopen / -pwgapext set them
+    ("blosum", True, {"CWREF_PWMATRIX": "blosum"}),
+    ("pam", True, {"CWREF_PWMATRIX": "pam"}),
+    ("id", True, {"CWREF_PWMATRIX": "id"}),
+    ("gonnet_go3_ge05", True, {"CWREF_PWGAPOPEN": "3.0", "CWREF_PWGAPEXT": "0.5"}),
+    ("blosum_go25_ge1", True, {"CWREF_PWMATRIX": "blosum", "CWREF_PWGAPOPEN": "25", "CWREF_PWGAPEXT": "1"}),
+    ("dna_go5_ge2", False, {"CWREF_PWGAPOPEN": "5", "CWREF_PWGAPEXT": "2"}),
+    ("dna_go40_ge0", False, {"CWREF_PWGAPOPEN": "40", "CWREF_PWGAPEXT": "0"}),
+]
+
+
+def make_pw_variants():
+    """Full-pairwise DistMatrices under the other pairwise matrices and gap
+    penalties (named pwparams_*: only the oracle test reads them)."""
+    prot = synth.to_fasta(synth.protein_family(30, 120, 41))
+    dna = synth.to_fasta(synth.dna_family(30, 150, 42))
+    for name, protein, ov in PW_VARIANTS:
+        save("pwparams_" + name, run_fasta(prot if protein else dna, name, overrides=ov))
+
+
 def main():
     O.build()
     mats = {}
@@ -234,6 +256,7 @@ def main():
     make_nj()
     make_fast()
     make_quick_limits()
+    make_pw_variants()
 
     os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
     with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
@@ -252,5 +275,8 @@ if __name__ == "__main__":
         O.build()
         make_limits()
         make_quick_limits()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--pw-variants":
+        O.build()
+        make_pw_variants()
     else:
         main()

@@ -4,10 +4,10 @@ edge cases (tests/golden/). Bit-exact: the reference stores a float in a double.
 import numpy as np
 import pytest
 
-from conftest import golden_names, load_big_golden, load_golden, range_pairs, sym_index
+from conftest import golden_names, load_big_golden, load_golden, pw_variant_names, range_pairs, sym_index
 
 
-@pytest.mark.parametrize("name", golden_names())
+@pytest.mark.parametrize("name", golden_names() + pw_variant_names())
 def test_oracle_matches_reference(name, oracle_mod):
     g = load_golden(name)
     n = len(g["seqs"])
