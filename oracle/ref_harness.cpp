@@ -15,7 +15,9 @@
 //        refharness --fast IN.fa OUT.bin [iStart iEnd jStart jEnd]
 //        refharness --nj IN.dist OUT.tree [OUT.report]
 // (CWREF_PWMATRIX, CWREF_PWGAPOPEN, CWREF_PWGAPEXT in the environment change the
-// pairwise matrix and gap penalties, see apply_overrides.)
+// pairwise matrix and gap penalties, see apply_overrides; CWREF_KTUP,
+// CWREF_WINDOW, CWREF_WINDOWGAP, CWREF_SIGNIF, CWREF_PERCENT the quick-distance
+// settings, see apply_quick_overrides.)
 //
 // --fast runs clustalw::FastPairwiseAlign::pairwiseAlign (the k-tuple quick
 // distances, pairwise/FastPairwiseAlign.cpp:20-139) instead; its OUT.bin starts
@@ -115,6 +117,34 @@ static void apply_overrides(bool dna) {
     }
 }
 
+// Quick-distance settings from the environment, stored as the per-type values
+// (AA* or DNA*, like the option parser does) that FastPairwiseAlign's own
+// setProtParams / setDNAParams call copies into the ones pairAlign reads
+// (FastPairwiseAlign.cpp:56-63, 176-183); the output file records what was used:
+//   CWREF_KTUP, CWREF_WINDOW, CWREF_WINDOWGAP, CWREF_SIGNIF (integers),
+//   CWREF_PERCENT (0 or 1)
+static void apply_quick_overrides(bool dna) {
+    int v = 0;
+    const char* e = getenv("CWREF_KTUP");
+    if (e && *e && sscanf(e, "%d", &v) == 1) {
+        if (dna) userParameters->setDNAKtup(v); else userParameters->setAAKtup(v);
+    }
+    e = getenv("CWREF_WINDOW");
+    if (e && *e && sscanf(e, "%d", &v) == 1) {
+        if (dna) userParameters->setDNAWindow(v); else userParameters->setAAWindow(v);
+    }
+    e = getenv("CWREF_WINDOWGAP");
+    if (e && *e && sscanf(e, "%d", &v) == 1) {
+        if (dna) userParameters->setDNAWindowGap(v); else userParameters->setAAWindowGap(v);
+    }
+    e = getenv("CWREF_SIGNIF");
+    if (e && *e && sscanf(e, "%d", &v) == 1) {
+        if (dna) userParameters->setDNASignif(v); else userParameters->setAASignif(v);
+    }
+    e = getenv("CWREF_PERCENT");
+    if (e && *e && sscanf(e, "%d", &v) == 1) userParameters->setPercent(v != 0);
+}
+
 static int run_nj(const char* in, const char* out, const char* report) {
     FILE* f = fopen(in, "rb");
     if (!f) return 4;
@@ -186,6 +216,7 @@ int main(int argc, char** argv) {
         return 3;
     }
     apply_overrides(userParameters->getDNAFlag());
+    apply_quick_overrides(userParameters->getDNAFlag());
     if (userParameters->getDNAFlag())
         userParameters->setDNAParams();
     else

@@ -49,7 +49,8 @@ def golden_names():
     start with nj_, quick k-tuple fixtures with fast_ or quicklimit_, other
     pairwise parameters with pwparams_, compact full-size ones with big_)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
-                  if f.endswith(".npz") and not f.startswith(("nj_", "fast_", "quicklimit_", "pwparams_", "big_")))
+                  if f.endswith(".npz")
+                  and not f.startswith(("nj_", "fast_", "quicklimit_", "quickparams_", "pwparams_", "big_")))
 
 
 def pw_variant_names():
@@ -102,6 +103,12 @@ def fast_golden_names():
 def quick_limit_names():
     """Quick-distance fixtures at the quick path's 8191-residue limit."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("quicklimit_") and f.endswith(".npz"))
+
+
+def quick_variant_names():
+    """Quick-distance fixtures under non-default ktup, window, window gap,
+    significance and percent settings."""
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.startswith("quickparams_") and f.endswith(".npz"))
 
 
 def load_fast_golden(name):

@@ -5,7 +5,7 @@ through oracle/_ref/refharness.
 Run from the repository root, where the reference tree is available:
     python tests/golden/make_golden.py
 (--nj-only, --fast-only, --limits or --pw-variants writes only the guide-tree,
-quick-distance, length-limit or pairwise-parameter fixtures.)
+quick-distance, length-limit or parameter-variant fixtures.)
 
 Each <name>.npz holds the encoded sequences exactly as the reference's reader
 produced them, the pairwise matrix and scalars the reference used, the range,
@@ -203,6 +203,34 @@ def make_pw_variants():
         save("pwparams_" + name, run_fasta(prot if protein else dna, name, overrides=ov))
 
 
+QUICK_VARIANTS = [
+    # (name, protein?, overrides): the quick-distance settings the GPU tests vary
+    ("prot_ktup2", True, {"CWREF_KTUP": "2"}),
+    ("prot_window1", True, {"CWREF_WINDOW": "1"}),
+    ("prot_window9_signif2", True, {"CWREF_WINDOW": "9", "CWREF_SIGNIF": "2"}),
+    ("prot_signif12", True, {"CWREF_SIGNIF": "12"}),
+    ("prot_windowgap1", True, {"CWREF_WINDOWGAP": "1"}),
+    ("prot_windowgap9", True, {"CWREF_WINDOWGAP": "9"}),
+    ("prot_percent0", True, {"CWREF_PERCENT": "0"}),
+    ("dna_ktup1", False, {"CWREF_KTUP": "1"}),
+    ("dna_ktup3", False, {"CWREF_KTUP": "3"}),
+    ("dna_ktup4", False, {"CWREF_KTUP": "4"}),
+]
+
+
+def make_quick_variants():
+    """Quick distances under non-default settings (named quickparams_*: only
+    the oracle test reads them)."""
+    prot = synth.to_fasta(synth.protein_family(24, 160, 31) + synth.protein_family(8, 40, 32))
+    dna = synth.to_fasta(synth.dna_family(20, 300, 41))
+    for name, protein, ov in QUICK_VARIANTS:
+        with tempfile.TemporaryDirectory() as d:
+            fa = os.path.join(d, "s.fa")
+            with open(fa, "w") as f:
+                f.write(prot if protein else dna)
+            save_fast("quickparams_" + name, O.run_reference(fa, os.path.join(d, "o.bin"), fast=True, overrides=ov))
+
+
 def main():
     O.build()
     mats = {}
@@ -257,6 +285,7 @@ def main():
     make_fast()
     make_quick_limits()
     make_pw_variants()
+    make_quick_variants()
 
     os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
     with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
@@ -278,5 +307,6 @@ if __name__ == "__main__":
     elif len(sys.argv) > 1 and sys.argv[1] == "--pw-variants":
         O.build()
         make_pw_variants()
+        make_quick_variants()
     else:
         main()

@@ -6,10 +6,10 @@ and DNA), a partial range, synthetic sets and protein/DNA edge cases
 import numpy as np
 import pytest
 
-from conftest import fast_golden_names, load_fast_golden, quick_limit_names, range_pairs, sym_index
+from conftest import fast_golden_names, load_fast_golden, quick_limit_names, quick_variant_names, range_pairs, sym_index
 
 
-@pytest.mark.parametrize("name", fast_golden_names() + quick_limit_names())
+@pytest.mark.parametrize("name", fast_golden_names() + quick_limit_names() + quick_variant_names())
 def test_fast_oracle_matches_reference(name, oracle_mod):
     g = load_fast_golden(name)
     n = len(g["seqs"])
