@@ -4,8 +4,9 @@ through oracle/_ref/refharness.
 
 Run from the repository root, where the reference tree is available:
     python tests/golden/make_golden.py
-(--nj-only, --fast-only, --limits or --pw-variants writes only the guide-tree,
-quick-distance, length-limit or parameter-variant fixtures.)
+(--nj-only, --fast-only, --limits, --pw-variants or --sequential writes only the
+guide-tree, quick-distance, length-limit, parameter-variant or src/sequential
+fixtures.)
 
 Each <name>.npz holds the encoded sequences exactly as the reference's reader
 produced them, the pairwise matrix and scalars the reference used, the range,
@@ -231,6 +232,26 @@ def make_quick_variants():
             save_fast("quickparams_" + name, O.run_reference(fa, os.path.join(d, "o.bin"), fast=True, overrides=ov))
 
 
+SEQUENTIAL = "/root/reference/CPU/clustalw-2.0.11/src/sequential"
+
+
+def make_sequential():
+    """The reference's other shipped inputs, src/sequential/100_{500,1000,1800}.fa
+    (protein; their .aln/.dnd are the reference's own CPU outputs): the whole
+    DistMatrix, filled in row ranges on all host cores (each range writes only
+    its own entries) and summed."""
+    from make_big_golden import run_ranges
+
+    k = os.cpu_count() or 4
+    for fx in ["100_500", "100_1000", "100_1800"]:
+        fasta = os.path.join(SEQUENTIAL, fx + ".fa")
+        with tempfile.TemporaryDirectory() as d:
+            n = int(O.run_reference(fasta, os.path.join(d, "meta.bin"), (0, 0, 0, 0))["n"])
+            ref, el = run_ranges(fasta, n, k, d)
+        ref = dict(ref, elements=el, range=np.array([0, n, 0, n], np.int32))
+        save("sequential_" + fx, ref)
+
+
 def main():
     O.build()
     mats = {}
@@ -286,6 +307,7 @@ def main():
     make_quick_limits()
     make_pw_variants()
     make_quick_variants()
+    make_sequential()
 
     os.makedirs(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data"), exist_ok=True)
     with open(os.path.join(REPO, "cuda-clustalw_gb300", "clustalw_gb300", "data", "pairwise_matrices.json"), "w") as f:
@@ -304,6 +326,9 @@ if __name__ == "__main__":
         O.build()
         make_limits()
         make_quick_limits()
+    elif len(sys.argv) > 1 and sys.argv[1] == "--sequential":
+        O.build()
+        make_sequential()
     elif len(sys.argv) > 1 and sys.argv[1] == "--pw-variants":
         O.build()
         make_pw_variants()
