@@ -128,7 +128,8 @@ def make_nj():
     plus small and tie-heavy matrices."""
     import glob
 
-    for path in sorted(glob.glob(os.path.join(OUT, "fixture_*.npz"))) + [os.path.join(OUT, "synth_uneven_40.npz")]:
+    for path in (sorted(glob.glob(os.path.join(OUT, "fixture_*.npz"))) + [os.path.join(OUT, "synth_uneven_40.npz")]
+                 + sorted(glob.glob(os.path.join(OUT, "sequential_*.npz")))):
         z = np.load(path)
         n = len(z["lens"])
         save_nj("nj_" + os.path.basename(path)[:-4], n, z["elements"])
