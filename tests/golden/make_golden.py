@@ -87,6 +87,9 @@ def make_fast():
                                                     fast=True))
         save_fast("fast_100_97_block", O.run_reference(os.path.join(FIXTURES, "100_97.fa"), os.path.join(d, "o.bin"),
                                                        (20, 60, 40, 70), fast=True))
+        for fx in ["100_500", "100_1000", "100_1800"]:
+            save_fast("fast_sequential_" + fx, O.run_reference(os.path.join(SEQUENTIAL, fx + ".fa"),
+                                                               os.path.join(d, "o.bin"), fast=True))
     for name, text in fast_sets():
         with tempfile.TemporaryDirectory() as d:
             fa = os.path.join(d, "s.fa")
