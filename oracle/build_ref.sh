@@ -26,7 +26,8 @@ general/VectorOutOfRange general/InvalidCombination general/DebugLog general/Sta
 general/ClustalWResources general/OutputFile fileInput/FileReader fileInput/FileParser
 fileInput/PearsonFileParser fileInput/InFileStream fileInput/MSFFileParser
 fileInput/PIRFileParser fileInput/RSFFileParser fileInput/GDEFileParser
-fileInput/ClustalFileParser fileInput/EMBLFileParser tree/NJTree"
+fileInput/ClustalFileParser fileInput/EMBLFileParser tree/NJTree
+tree/UnRootedClusterTree tree/ClusterTree tree/ClusterTreeOutput tree/RandomGenerator"
 OBJS=""
 for u in $UNITS; do
     o="$OUT/obj/$(basename "$u").o"

@@ -14,6 +14,7 @@
 // Usage: refharness IN.fa OUT.bin [iStart iEnd jStart jEnd]
 //        refharness --fast IN.fa OUT.bin [iStart iEnd jStart jEnd]
 //        refharness --nj IN.dist OUT.tree [OUT.report]
+//        refharness --dnd IN.fa IN.dist OUT.dnd
 // (CWREF_PWMATRIX, CWREF_PWGAPOPEN, CWREF_PWGAPEXT in the environment change the
 // pairwise matrix and gap penalties, see apply_overrides; CWREF_KTUP,
 // CWREF_WINDOW, CWREF_WINDOWGAP, CWREF_SIGNIF, CWREF_PERCENT the quick-distance
@@ -61,6 +62,7 @@
 #include "pairwise/FullPairwiseAlign.h"
 #include "substitutionMatrix/SubMatrix.h"
 #include "tree/NJTree.h"
+#include "tree/UnRootedClusterTree.h"
 
 namespace clustalw {
 UserParameters* userParameters;
@@ -185,6 +187,33 @@ static int run_nj(const char* in, const char* out, const char* report) {
     return 0;
 }
 
+// --dnd: the guide-tree file Clustal::align writes after the pairwise stage
+// (TreeInterface::generateTreeFromDistMatNJ -> UnRootedClusterTree::
+// treeFromDistMatrix, tree/TreeInterface.cpp:418-430, tree/UnRootedClusterTree.cpp:
+// 171-260), from a given DistMatrix (IN.dist: int32 n, then the packed
+// elements) and the sequence names of IN.fa.
+static int run_dnd(const char* fasta, const char* dist_in, const char* out) {
+    userParameters->setDisplayInfo(false);
+    userParameters->setSeqName(std::string(fasta));
+    Alignment aln;
+    FileReader reader;
+    if (reader.readSeqs(&aln, 1) != OK) return 3;
+    const int n = aln.getNumSeqs();
+    FILE* f = fopen(dist_in, "rb");
+    if (!f) return 4;
+    int n2 = 0;
+    if (fread(&n2, sizeof(int), 1, f) != 1 || n2 != n) return 5;
+    SymMatrix dist;
+    dist.ResizeRect(n + 1);
+    const size_t nel = (size_t)(n + 1) * (n + 2) / 2;
+    if (fread(dist.getElements(), sizeof(double), nel, f) != nel) return 5;
+    fclose(f);
+    std::string name(out);
+    UnRootedClusterTree tree;
+    tree.treeFromDistMatrix(&dist, &aln, 1, n, name);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     bool fast = false;
     if (argc > 1 && std::string(argv[1]) == "--fast") {
@@ -196,6 +225,13 @@ int main(int argc, char** argv) {
         userParameters = new UserParameters(false);
         utilityObject = new Utility();
         return run_nj(argv[2], argv[3], argc == 5 ? argv[4] : 0);
+    }
+    if (argc == 5 && std::string(argv[1]) == "--dnd") {
+        userParameters = new UserParameters(false);
+        utilityObject = new Utility();
+        subMatrix = new SubMatrix();
+        statsObject = new Stats();
+        return run_dnd(argv[2], argv[3], argv[4]);
     }
     if (argc != 3 && argc != 7) {
         fprintf(stderr, "usage: %s IN.fa OUT.bin [iStart iEnd jStart jEnd]\n", argv[0]);

@@ -1,6 +1,9 @@
 """The oracle restatement (oracle/oracle.c) against distance matrices written by
 the unmodified reference on its own fixtures, partial ranges, synthetic sets and
 edge cases (tests/golden/). Bit-exact: the reference stores a float in a double."""
+import os
+import subprocess
+
 import numpy as np
 import pytest
 
@@ -29,12 +32,10 @@ def test_gap_penalties_match_reference_types(oracle_mod):
     assert oracle_mod.gap_penalties(prot, 1523, 1600)[0] == 2841
 
 
-def test_oracle_matches_reference_on_1000_97(oracle_mod):
-    """The oracle on the reference's own 1000 x 97 test set, all 499,500
-    pairs: the DistMatrix it fills hashes to what the unmodified reference
-    filled (the larger compact fixtures are checked on the GPU only)."""
-    import hashlib
-
+@pytest.fixture(scope="module")
+def oracle_1000_97(oracle_mod):
+    """The oracle's whole DistMatrix of the reference's 1000 x 97 test set
+    (499,500 pairs), computed once for the tests below."""
     g = load_big_golden("big_1000_97")
     n = len(g["seqs"])
     pairs = range_pairs(n, *g["range"])
@@ -42,6 +43,16 @@ def test_oracle_matches_reference_on_1000_97(oracle_mod):
     el = np.zeros(g["n_elements"])
     si, sj = pairs[:, 0].astype(np.int64), pairs[:, 1].astype(np.int64)
     el[(sj * (sj + 1)) // 2 + si] = r["dist"].astype(np.float64)
+    return g, el
+
+
+def test_oracle_matches_reference_on_1000_97(oracle_1000_97):
+    """The oracle on the reference's own 1000 x 97 test set, all 499,500
+    pairs: the DistMatrix it fills hashes to what the unmodified reference
+    filled (the larger compact fixtures are checked on the GPU only)."""
+    import hashlib
+
+    g, el = oracle_1000_97
     assert np.array_equal(el[g["sample_idx"]].view(np.int64), g["sample_val"].view(np.int64))
     assert hashlib.sha256(np.ascontiguousarray(el, dtype="<f8").tobytes()).digest() == g["sha256"]
 
@@ -80,23 +91,69 @@ def test_oracle_quick_matches_reference_samples_full_size(oracle_mod, name):
     assert np.array_equal(np.asarray(r["dist"], np.float64).view(np.int64), x["fast_sample_val"].view(np.int64))
 
 
-def test_oracle_tree_matches_reference_on_1000_97(oracle_mod):
+def test_oracle_tree_matches_reference_on_1000_97(oracle_mod, oracle_1000_97):
     """The oracle's guide tree on the reference's 1000 x 97 DistMatrix (itself
     checked by hash above) hashes to what the unmodified NJTree leaves."""
     import hashlib
 
     from conftest import load_big_extra
 
-    g = load_big_golden("big_1000_97")
+    g, el = oracle_1000_97
     x = load_big_extra("big_1000_97")
     n = len(g["seqs"])
-    pairs = range_pairs(n, *g["range"])
-    r = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
-    el = np.zeros(g["n_elements"])
-    si, sj = pairs[:, 0].astype(np.int64), pairs[:, 1].astype(np.int64)
-    el[(sj * (sj + 1)) // 2 + si] = r["dist"].astype(np.float64)
-    left, right, desc, el_after = oracle_mod.nj_tree(n, el)
+    left, right, desc, el_after = oracle_mod.nj_tree(n, el.copy())
     h = hashlib.sha256()
     for a in (np.asarray(left, "<f8"), np.asarray(right, "<f8"), np.asarray(desc, "<i4"), np.asarray(el_after, "<f8")):
         h.update(np.ascontiguousarray(a).tobytes())
     assert h.digest() == x["nj_sha256"]
+
+
+REF_TREE = os.environ.get("CLUSTALW_REF_ROOT", "/root/reference")
+SHIPPED_DND = {
+    # fixture -> the reference's shipped input / guide-tree pair (its own CPU outputs)
+    "fixture_100_97": "test_data/correct/100_97",
+    "fixture_100_498": "test_data/correct/100_498",
+    "fixture_100_1002": "test_data/correct/100_1002",
+    "fixture_100_1523": "test_data/correct/100_1523",
+    "sequential_100_500": "CPU/clustalw-2.0.11/src/sequential/100_500",
+    "sequential_100_1000": "CPU/clustalw-2.0.11/src/sequential/100_1000",
+    "sequential_100_1800": "CPU/clustalw-2.0.11/src/sequential/100_1800",
+    "big_1000_97": "test_data/correct/1000_97",
+}
+
+
+def _dnd_from(elements, n, base, tmp_path):
+    from oracle import oracle as O
+
+    dist = tmp_path / "in.dist"
+    out = tmp_path / "out.dnd"
+    with open(dist, "wb") as f:
+        f.write(np.int32(n).tobytes())
+        f.write(np.asarray(elements, "<f8").tobytes())
+    subprocess.run([O.REF_HARNESS, "--dnd", base + ".fa", str(dist), str(out)], check=True,
+                   stdout=subprocess.DEVNULL)
+    return out.read_text()
+
+
+@pytest.mark.skipif(not os.path.isdir(os.path.join(REF_TREE, "test_data")), reason="reference tree not present")
+@pytest.mark.parametrize("name", sorted(SHIPPED_DND))
+def test_distances_reproduce_the_shipped_guide_trees(name, tmp_path, oracle_mod, request):
+    """The reference's shipped guide-tree files (.dnd, its own CPU outputs for
+    these inputs) come out byte for byte when the reference's own tree code
+    (UnRootedClusterTree::treeFromDistMatrix through oracle/_ref/refharness
+    --dnd) runs on the DistMatrix the oracle reproduces: the stored fixture
+    (equal to the oracle's, tested above) or, for 1000_97, the oracle's own."""
+    from oracle import oracle as O
+
+    if not os.path.exists(O.REF_HARNESS):
+        pytest.skip("reference harness not built")
+    base = os.path.join(REF_TREE, SHIPPED_DND[name])
+    if name == "big_1000_97":
+        g, el = request.getfixturevalue("oracle_1000_97")
+        n = len(g["seqs"])
+    else:
+        g = load_golden(name)
+        el, n = g["elements"], len(g["seqs"])
+    with open(base + ".dnd") as f:
+        want = f.read()
+    assert _dnd_from(el, n, base, tmp_path) == want
