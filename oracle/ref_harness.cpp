@@ -241,7 +241,11 @@ int main(int argc, char** argv) {
     utilityObject = new Utility();
     subMatrix = new SubMatrix();
     statsObject = new Stats();
-    userParameters->setDisplayInfo(false);
+    // CWREF_DISPLAY_INFO=1: the per-pair info lines of FullPairwiseAlign.cpp:185-189
+    // (and FastPairwiseAlign's) go to standard output, as clustalw2 prints them
+    // without -QUIET.
+    const char* disp = getenv("CWREF_DISPLAY_INFO");
+    userParameters->setDisplayInfo(disp && *disp == '1');
     userParameters->setSeqName(std::string(argv[1]));
 
     Alignment aln;

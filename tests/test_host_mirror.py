@@ -3,7 +3,9 @@
 error behaviour for a wrong matrix size and bad ranges (message + exit 1, no
 device work), residue encoding, and -- on the GPU -- pairwiseAlign filling a
 DistMatrix exactly as the reference's FullPairwiseAlign did (golden fixtures,
-full and partial ranges), with the same per-pair info lines."""
+full and partial ranges), with the same per-pair info lines; on the CPU, the
+info lines built from per-pair identity counts equal the ones the unmodified
+reference prints."""
 import numpy as np
 import pytest
 
@@ -88,3 +90,43 @@ def test_info_lines(capsys):
         score = int(line.rsplit(" ", 1)[1])
         d = dm.GetAt(i, j)
         assert abs((100.0 - 100.0 * d) - score) < 1.0 + 1e-4
+
+
+INFO_LINE = r"Sequences \((\d+):(\d+)\) Aligned\. Score:  (-?\d+)"
+
+
+@pytest.mark.parametrize("name,rng", [("fixture_100_97", None), ("edge_protein", None),
+                                      ("fixture_100_97", (10, 30, 5, 60))])
+def test_info_lines_match_the_reference(name, rng, tmp_path, capsys, oracle_mod):
+    """The per-pair lines the mirror prints when display is on
+    (FullPairwiseAlign.cpp:185-189, the "Score" known answers clustalw2 prints
+    without -QUIET), built from the per-pair identity counts the GPU returns
+    (here the oracle's, which the GPU tests equal), are the lines the
+    unmodified reference prints (oracle/_ref/refharness with
+    CWREF_DISPLAY_INFO=1), pair for pair. CPU only; needs the harness."""
+    import os
+    import re
+    import subprocess
+
+    from clustalw_gb300 import synth
+    from clustalw_gb300.pairwise import Alignment, FullPairwiseAlign, PairwiseSettings
+    from conftest import range_pairs
+
+    if not os.path.exists(oracle_mod.REF_HARNESS):
+        pytest.skip("reference harness not built")
+    g = load_golden(name)
+    n = len(g["seqs"])
+    rng = rng or (0, n, 0, n)
+    fa = tmp_path / "in.fa"
+    fa.write_text(synth.to_fasta(g["seqs"]))
+    out = subprocess.run([oracle_mod.REF_HARNESS, str(fa), str(tmp_path / "o.bin"), *map(str, rng)],
+                         capture_output=True, text=True, check=True, env=dict(os.environ, CWREF_DISPLAY_INFO="1"))
+    ref = oracle_mod.read_ref_output(str(tmp_path / "o.bin"))
+    assert all(np.array_equal(a, b) for a, b in zip(ref["seqs"], g["seqs"]))  # the reader saw the same codes
+    want = re.findall(INFO_LINE, out.stdout)
+    pairs = range_pairs(n, *rng)
+    stats = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    capsys.readouterr()
+    FullPairwiseAlign(PairwiseSettings(g["matrix"], g["params"]))._print_info(Alignment(g["seqs"]), stats, *rng)
+    got = re.findall(INFO_LINE, capsys.readouterr().out)
+    assert len(want) > 0 and got == want
