@@ -130,3 +130,44 @@ def test_info_lines_match_the_reference(name, rng, tmp_path, capsys, oracle_mod)
     FullPairwiseAlign(PairwiseSettings(g["matrix"], g["params"]))._print_info(Alignment(g["seqs"]), stats, *rng)
     got = re.findall(INFO_LINE, capsys.readouterr().out)
     assert len(want) > 0 and got == want
+
+
+# the reference writes the newline before each line, so the last one runs into
+# what follows: the score is matched as a %g number
+QUICK_LINE = r"Sequences \((\d+):(\d+)\) (Aligned\. Score: \d+(?:\.\d+)?(?:e[-+]\d+)?|Not Aligned)"
+
+
+@pytest.mark.parametrize("name,rng", [("fast_100_97", None), ("fast_edge_protein", None), ("fast_edge_dna", None),
+                                      ("fast_100_97_block", None)])
+def test_quick_info_lines_match_the_reference(name, rng, tmp_path, capsys, oracle_mod):
+    """The quick path's per-pair lines (FastPairwiseAlign.cpp:110-120, "%lg"
+    scores and "Not Aligned"), built by the mirror from per-pair best scores
+    (the oracle's, which the GPU tests equal), are the lines the unmodified
+    reference prints. CPU only; needs the harness."""
+    import os
+    import re
+    import subprocess
+
+    from clustalw_gb300 import synth
+    from clustalw_gb300.native import FastParams
+    from clustalw_gb300.pairwise import Alignment, FastPairwiseAlign
+    from conftest import load_fast_golden, range_pairs
+
+    if not os.path.exists(oracle_mod.REF_HARNESS):
+        pytest.skip("reference harness not built")
+    g = load_fast_golden(name)
+    n = len(g["seqs"])
+    rng = tuple(g["range"])
+    fa = tmp_path / "in.fa"
+    fa.write_text(synth.to_fasta(g["seqs"]))
+    out = subprocess.run([oracle_mod.REF_HARNESS, "--fast", str(fa), str(tmp_path / "o.bin"), *map(str, rng)],
+                         capture_output=True, text=True, check=True, env=dict(os.environ, CWREF_DISPLAY_INFO="1"))
+    ref = oracle_mod.read_ref_output(str(tmp_path / "o.bin"))
+    assert all(np.array_equal(a, b) for a, b in zip(ref["seqs"], g["seqs"]))
+    want = re.findall(QUICK_LINE, out.stdout)
+    stats = oracle_mod.fast_pairs(g["seqs"], g["fast_params"], range_pairs(n, *rng))
+    capsys.readouterr()
+    fp = FastParams.from_dict(g["fast_params"])
+    FastPairwiseAlign(fp)._print_info(Alignment(g["seqs"]), fp, stats, *rng)
+    got = re.findall(QUICK_LINE, capsys.readouterr().out)
+    assert len(want) > 0 and got == want
