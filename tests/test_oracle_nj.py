@@ -52,3 +52,29 @@ def test_nj_report_matches_reference(name, oracle_mod):
     n = int(g["n"])
     left, right, _, _, joins = oracle_mod.nj_tree(n, g["elements"], want_joins=True)
     assert _REPORT_HEAD + nj_report(n, joins, left, right) == str(g["report"])
+
+
+@pytest.mark.parametrize("d", [0.0412371047, 0.0, 0.5, 1.0])
+def test_two_sequence_tree_matches_reference(d, tmp_path, oracle_mod):
+    """Two sequences: the reference writes one report line and returns before
+    touching the tree (NJTree.cpp:218-229); the mirror's NJTree does the same
+    without a device call. Report text against the unmodified reference."""
+    import io
+    import os
+
+    from clustalw_gb300.pairwise import DistMatrix
+    from clustalw_gb300.tree import NJTree, PhyloTree, SeqInfo
+
+    if not os.path.exists(oracle_mod.REF_HARNESS):
+        pytest.skip("reference harness not built")
+    el = np.zeros(6)
+    el[1] = float(np.float32(d))  # getIndex(1, 2): the float the pairwise stage stores
+    *_, report = oracle_mod.run_reference_nj(2, el, str(tmp_path), report=True)
+    dm = DistMatrix(3)
+    dm.getElements()[:] = el
+    tree, out = PhyloTree(), io.StringIO()
+    nj = NJTree(gpu=object())  # never used for two sequences
+    nj.setVerbose(True)
+    nj.generateTree(tree, dm, SeqInfo(1, 2, 2), out)
+    assert out.getvalue() == report
+    assert len(tree.leftBranch) == 0 and len(tree.rightBranch) == 0
