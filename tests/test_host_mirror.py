@@ -52,6 +52,27 @@ def test_reference_error_behaviour(capsys):
     fpa.pairwiseAlign(Alignment([]), DistMatrix(1), 0, 0, 0, 0)
 
 
+
+def test_quick_mirror_error_behaviour(capsys):
+    """FastPairwiseAlign's mirror rejects a wrong matrix size and bad ranges
+    with the reference's messages and exit status 1 (FastPairwiseAlign.cpp:
+    24-35), before any device work."""
+    from clustalw_gb300.pairwise import Alignment, DistMatrix, FastPairwiseAlign
+
+    g = load_golden("synth_uneven_40")
+    aln = Alignment(g["seqs"][:5])
+    fpa = FastPairwiseAlign()
+    with pytest.raises(SystemExit) as e:
+        fpa.pairwiseAlign(aln, DistMatrix(5), 0, 5, 0, 5)
+    assert e.value.code == 1
+    assert capsys.readouterr().out == "The distance matrix is not the right size!\nNeed to terminate program.\n"
+    for rng in [(-1, 5, 0, 5), (3, 2, 0, 5), (0, 5, -1, 5), (0, 5, 4, 3)]:
+        with pytest.raises(SystemExit) as e:
+            fpa.pairwiseAlign(aln, DistMatrix(6), *rng)
+        assert e.value.code == 1
+        assert capsys.readouterr().out == "The range for pairwise Alignment is incorrect.\nNeed to terminate program.\n"
+
+
 def test_encode_decode():
     from clustalw_gb300.pairwise import GAP_POS2, decode, encode
 
