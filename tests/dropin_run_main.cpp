@@ -11,6 +11,8 @@
 //   KIND nj: the full DistMatrix from the reference FullPairwiseAlign, then the
 //   tree plugin with its verbose report written to OUT.bin.report; OUT.bin
 //   holds leftBranch, rightBranch, treeDesc and the joined matrix.
+// The CWREF_* variables of oracle/ref_overrides.h set the pairwise matrix, gap
+// penalties and quick-distance settings for both implementations alike.
 #include <cstdio>
 #include <cstdlib>
 #include <fstream>
@@ -42,6 +44,8 @@ Stats* statsObject;
 
 using namespace clustalw;
 
+#include "ref_overrides.h"  // CWREF_* parameter settings from the environment
+
 static void put(FILE* f, const void* p, size_t n) {
     if (n && fwrite(p, 1, n, f) != n) exit(2);
 }
@@ -61,6 +65,8 @@ int main(int argc, char** argv) {
     Alignment aln;
     FileReader reader;
     if (reader.readSeqs(&aln, 1) != OK) return 3;
+    apply_overrides(userParameters->getDNAFlag());
+    apply_quick_overrides(userParameters->getDNAFlag());
     if (userParameters->getDNAFlag())
         userParameters->setDNAParams();
     else

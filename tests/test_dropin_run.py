@@ -36,6 +36,7 @@ def runner(tmp_path_factory, oracle_mod):
     out = str(d / "dropin_run")
     subprocess.run(["g++", "-std=gnu++98", "-w", "-DOS_UNIX=1", "-I" + REF_SRC,
                     "-I" + os.path.join(REPO, "oracle", "_ref", "include"), "-I" + os.path.join(REPO, "include"),
+                    "-I" + os.path.join(REPO, "oracle"),
                     "-I" + host, os.path.join(host, "GpuFullPairwiseAlign.cpp"),
                     os.path.join(host, "GpuFastPairwiseAlign.cpp"), os.path.join(host, "GpuNJTree.cpp"),
                     os.path.join(REPO, "tests", "dropin_run_main.cpp"), *objs, stub, "-lpthread", "-lm", "-o", out],
@@ -57,12 +58,13 @@ def fasta_of(name, tmp_path):
     return str(path)
 
 
-def run_both(runner, kind, fasta, tmp_path, rng=()):
+def run_both(runner, kind, fasta, tmp_path, rng=(), overrides=None):
     outs = {}
+    env = dict(os.environ, **(overrides or {}))
     for impl in ("ref", "dropin"):
         bin_path = tmp_path / f"{impl}_{kind}.bin"
         r = subprocess.run([runner, impl, kind, fasta, str(bin_path), *map(str, rng)], capture_output=True,
-                           check=True)
+                           check=True, env=env)
         report = bin_path.with_name(bin_path.name + ".report")
         outs[impl] = (bin_path.read_bytes(), r.stdout, report.read_bytes() if report.exists() else b"")
     return outs
@@ -86,3 +88,22 @@ def test_dropin_tree_leaves_what_the_reference_leaves(runner, source, tmp_path):
     outs = run_both(runner, "nj", fasta_of(source, tmp_path), tmp_path)
     assert len(outs["ref"][2]) > 0  # the verbose report was written
     assert outs["dropin"] == outs["ref"]  # tree, joined matrix, standard output, report
+
+
+@pytest.mark.parametrize("kind,source,overrides", [
+    ("full", "shipped:test_data/correct/100_97.fa", {"CWREF_PWMATRIX": "blosum", "CWREF_PWGAPOPEN": "3",
+                                                     "CWREF_PWGAPEXT": "0.5"}),
+    ("full", "shipped:test_data/correct/100_97.fa", {"CWREF_PWMATRIX": "id"}),
+    ("full", "synth_dna_40x300", {"CWREF_PWGAPOPEN": "40", "CWREF_PWGAPEXT": "0"}),
+    ("fast", "shipped:test_data/correct/100_97.fa", {"CWREF_KTUP": "2", "CWREF_WINDOW": "9", "CWREF_SIGNIF": "2"}),
+    ("fast", "shipped:test_data/correct/100_97.fa", {"CWREF_PERCENT": "0", "CWREF_WINDOWGAP": "9"}),
+    ("fast", "synth_dna_40x300", {"CWREF_KTUP": "3"}),
+])
+def test_dropin_reads_the_reference_settings(runner, kind, source, overrides, tmp_path):
+    """Under non-default pairwise matrices, gap penalties and quick-distance
+    settings (set in userParameters / subMatrix, as clustalw2's options do) the
+    drop-ins still leave what the reference classes leave: they read those
+    settings where the reference reads them."""
+    outs = run_both(runner, kind, fasta_of(source, tmp_path), tmp_path, overrides=overrides)
+    assert outs["dropin"][0] == outs["ref"][0]
+    assert outs["dropin"][1] == outs["ref"][1]
