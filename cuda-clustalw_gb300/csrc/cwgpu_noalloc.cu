@@ -7,7 +7,7 @@
 // can still hand over device buffers they already own. This entry point runs
 // the same pair kernel as cwgpu_align_pairs, but every byte of working memory
 // it needs (per-warp boundary rows, the queue head, the cell counters, the
-// status word and the gap-open table) lives in one file-scope static device
+// status words and the gap-open table) lives in one file-scope static device
 // array, g_noalloc_scratch, of CWGPU_NOALLOC_SCRATCH_BYTES (16 MiB). Every GPU that
 // loads this library holds that array until the process exits.
 //
@@ -34,7 +34,10 @@ namespace {
 constexpr int kNaWarpsPerBlock = 4;
 constexpr size_t kNaRegionBytes = (size_t)cwgpu::warp_region_bytes(CWGPU_NUMRES);  // per warp, dynamic smem
 constexpr size_t kNaScratchBytes = (size_t)CWGPU_NOALLOC_SCRATCH_BYTES;
-constexpr size_t kNaCtrlBytes = 256;  // [0] queue head, [1..3] cell counts, [4] status word
+// Control words: [0] queue head, [1..3] cell counts, then three status words
+// (int): rejected input, matrix entry outside int16, device-side limit.
+constexpr size_t kNaCtrlBytes = 256;
+constexpr int kNaStatusInput = 0, kNaStatusMatrix = 1, kNaStatusLimit = 2;
 constexpr size_t kNaTableBytes = ((size_t)(CWGPU_NOALLOC_MAX_LEN + 1) * sizeof(int32_t) + 255) & ~(size_t)255;
 constexpr size_t kNaRowsOffset = kNaCtrlBytes + kNaTableBytes;
 
@@ -56,15 +59,19 @@ struct NaArgs {
     int gp1, gp2;
 };
 
+__device__ __forceinline__ int* na_status(unsigned char* scratch, int which) {
+    return reinterpret_cast<int*>(scratch + 4 * sizeof(unsigned long long)) + which;
+}
+
 // One pair (FullPairwiseAlign.cpp:112-183) with device-side input checks: a
-// pair index, a length above max_len or a residue code outside [0, 31] sets
-// the status word and the pair is skipped. The residue counts len1/len2 of
-// :100-127 are counted here instead of being uploaded.
+// pair index, a negative sequence offset, a length above max_len or a residue
+// code outside [0, 31] sets the input status word and the pair is skipped. The
+// residue counts len1/len2 of :100-127 are counted here instead of being
+// uploaded.
 __device__ void na_align_pair(const NaArgs& a, long long q, const cwgpu::Env& X, int2* bufA, int2* bufB,
                               unsigned long long (&acc)[3]) {
     const int lane = threadIdx.x & 31;
-    unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(a.scratch);
-    int* status = reinterpret_cast<int*>(ctrl + 4);
+    int* status = na_status(a.scratch, kNaStatusInput);
     const int32_t* go_table = reinterpret_cast<const int32_t*>(a.scratch + kNaCtrlBytes);
     const int si = a.pairs[2 * q], sj = a.pairs[2 * q + 1];
     if (si < 0 || si >= a.nseqs || sj < 0 || sj >= a.nseqs) {
@@ -72,7 +79,7 @@ __device__ void na_align_pair(const NaArgs& a, long long q, const cwgpu::Env& X,
         return;
     }
     const int n = a.lens[si], m = a.lens[sj];
-    if (n < 0 || m < 0 || n > a.max_len || m > a.max_len) {
+    if (n < 0 || m < 0 || n > a.max_len || m > a.max_len || (n > 0 && a.offs[si] < 0) || (m > 0 && a.offs[sj] < 0)) {
         if (lane == 0) atomicExch(status, 1);
         return;
     }
@@ -102,11 +109,23 @@ __device__ void na_align_pair(const NaArgs& a, long long q, const cwgpu::Env& X,
     }
 }
 
+// The matrix is checked while it is staged: the score profile holds int16
+// entries, so an entry outside [-32768, 32767] sets the matrix status word and
+// every block returns before aligning anything (cwgpu_set_matrix makes the same
+// check on the host for the allocating entry points).
 __global__ void __launch_bounds__(kNaWarpsPerBlock * 32) k_pairwise_noalloc(NaArgs a) {
     __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
     extern __shared__ __align__(16) uint16_t na_region[];
-    for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = a.matrix[i];
-    __syncthreads();
+    int bad_entry = 0;
+    for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) {
+        const int v = a.matrix[i];
+        bad_entry |= (v < -32768 || v > 32767);
+        smat[i] = v;
+    }
+    if (__syncthreads_or(bad_entry)) {
+        if (threadIdx.x == 0) atomicExch(na_status(a.scratch, kNaStatusMatrix), 1);
+        return;
+    }
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const long long slot = (long long)blockIdx.x * kNaWarpsPerBlock + warp;
     cwgpu::Env X;
@@ -118,7 +137,7 @@ __global__ void __launch_bounds__(kNaWarpsPerBlock * 32) k_pairwise_noalloc(NaAr
     X.tiny_m = 32;
     X.tiny_n = cwgpu::kTinyMaxN;
     unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(a.scratch);
-    X.err = reinterpret_cast<int*>(ctrl + 4);
+    X.err = na_status(a.scratch, kNaStatusLimit);
     int2* rows = reinterpret_cast<int2*>(a.scratch + kNaRowsOffset);
     int2* bufA = rows + (size_t)slot * 2 * (a.max_len + 1);
     int2* bufB = bufA + (a.max_len + 1);
@@ -248,14 +267,25 @@ extern "C" int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d
         k_pairwise_noalloc<<<(unsigned)grid, kNaWarpsPerBlock * 32, kNaRegionBytes * kNaWarpsPerBlock, s>>>(a);
         e = cudaGetLastError();
     }
-    int status = 0;
+    int status[3] = {0, 0, 0};
     if (e == cudaSuccess)
-        e = cudaMemcpyAsync(&status, d->scratch + 4 * sizeof(unsigned long long), sizeof(int), cudaMemcpyDeviceToHost, s);
+        e = cudaMemcpyAsync(status, d->scratch + 4 * sizeof(unsigned long long), sizeof(status),
+                            cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) {
         fprintf(stderr, "cwgpu_align_pairs_noalloc: %s\n", cudaGetErrorString(e));
         return CWGPU_ERR_CUDA;
     }
-    if (status) return na_reject("input rejected on the device (pair index, length above max_len, or residue code)");
+    if (status[kNaStatusMatrix]) {
+        fprintf(stderr, "cwgpu_align_pairs_noalloc: matrix entry outside the int16 profile range\n");
+        return CWGPU_ERR_MATRIX;
+    }
+    if (status[kNaStatusInput])
+        return na_reject("input rejected on the device (pair index, sequence offset, length above max_len, or "
+                         "residue code)");
+    if (status[kNaStatusLimit]) {
+        fprintf(stderr, "cwgpu_align_pairs_noalloc: device-side limit reached (Myers-Miller stack depth)\n");
+        return CWGPU_ERR_DEVICE;
+    }
     return CWGPU_OK;
 }

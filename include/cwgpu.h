@@ -133,8 +133,9 @@ int cwgpu_pairwise_align(cwgpu_context* ctx, int32_t i_start, int32_t i_end, int
 
 /* Aligns an explicit host pair list: pairs[2q] = si (row sequence, the
  * reference's seq1), pairs[2q+1] = sj. Writes dist_out[q] (the float the
- * reference stores with SetAt) and, if not NULL, stats_out[q]. One persistent,
- * graph-captured, length-ordered launch. */
+ * reference stores with SetAt) and, if not NULL, stats_out[q]. The same
+ * persistent, length-ordered launches as a plan, enqueued directly on the
+ * context's streams (no graph is built for a one-shot call). */
 int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,
                       cwgpu_pair_stats* stats_out);
 
@@ -188,8 +189,11 @@ void cwgpu_plan_destroy(cwgpu_plan* plan);
  * address and should come before any stream capture. The call waits for its
  * kernel on `stream` (a cudaStream_t, NULL = legacy default) and returns
  * CWGPU_ERR_ARG if the device-side checks rejected an input (pair index,
- * length above max_len, residue code outside [0, 31]). Calls share the array:
- * calls whose GPU work overlaps race. */
+ * negative sequence offset, length above max_len, residue code outside
+ * [0, 31]), CWGPU_ERR_MATRIX if a d_matrix entry is outside int16 (nothing is
+ * aligned then), CWGPU_ERR_DEVICE if a pair reached the Myers-Miller stack
+ * limit. Calls share the array: calls whose GPU work overlaps race, so callers
+ * serialise them (one stream, or calls that do not overlap). */
 #define CWGPU_NOALLOC_MAX_LEN 8191
 #define CWGPU_NOALLOC_SCRATCH_BYTES (16u << 20)
 int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d_offsets, const int32_t* d_lens,

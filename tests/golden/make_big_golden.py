@@ -33,7 +33,8 @@ sys.path.insert(0, REPO)
 
 from oracle import oracle as O  # noqa: E402
 
-FIXTURES = "/root/reference/test_data/correct"
+REF_ROOT = os.environ.get("CLUSTALW_REF_ROOT", "/root/reference")
+FIXTURES = os.path.join(REF_ROOT, "test_data", "correct")
 OUT = os.path.dirname(os.path.abspath(__file__))
 NAMES = ["1000_97", "1000_498", "1000_1002", "1000_1523"]
 

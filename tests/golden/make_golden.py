@@ -28,7 +28,8 @@ sys.path.insert(0, os.path.join(REPO, "cuda-clustalw_gb300"))
 from clustalw_gb300 import synth  # noqa: E402
 from oracle import oracle as O  # noqa: E402
 
-FIXTURES = "/root/reference/test_data/correct"
+REF_ROOT = os.environ.get("CLUSTALW_REF_ROOT", "/root/reference")
+FIXTURES = os.path.join(REF_ROOT, "test_data", "correct")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
@@ -236,7 +237,7 @@ def make_quick_variants():
             save_fast("quickparams_" + name, O.run_reference(fa, os.path.join(d, "o.bin"), fast=True, overrides=ov))
 
 
-SEQUENTIAL = "/root/reference/CPU/clustalw-2.0.11/src/sequential"
+SEQUENTIAL = os.path.join(REF_ROOT, "CPU", "clustalw-2.0.11", "src", "sequential")
 
 
 def make_sequential():

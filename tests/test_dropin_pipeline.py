@@ -1,5 +1,5 @@
-"""The whole clustalw2 program with the drop-ins bound in, exactly as
-INTEGRATION.md describes (in a temporary copy of Clustal.cpp, `new
+"""The whole clustalw2 program with the drop-ins bound in by the maintainer's
+two-line edit (in a temporary copy of Clustal.cpp, `new
 FullPairwiseAlign()` becomes `new GpuFullPairwiseAlign(0)` and `new
 FastPairwiseAlign()` becomes `new GpuFastPairwiseAlign(0)`; every other
 reference source compiles unchanged), writes the reference's shipped alignment
@@ -25,7 +25,8 @@ pytestmark = pytest.mark.skipif(not os.path.isdir(CORRECT), reason="reference tr
 
 
 def bind_dropins(text):
-    """The maintainer's edit of Clustal.cpp."""
+    """The maintainer's edit of Clustal.cpp: construct the drop-ins where the
+    reference constructs FullPairwiseAlign and FastPairwiseAlign."""
     text = text.replace("new FullPairwiseAlign()", "new GpuFullPairwiseAlign(0)")
     text = text.replace("new FastPairwiseAlign()", "new GpuFastPairwiseAlign(0)")
     return text.replace('#include "pairwise/FastPairwiseAlign.h"',

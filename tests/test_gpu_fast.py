@@ -7,7 +7,7 @@ repeats (the reference's quicksort decides the selected diagonals) and the
 import numpy as np
 import pytest
 
-from conftest import fast_golden_names, load_fast_golden, range_pairs, sym_index
+from conftest import fast_golden_names, load_fast_golden, quick_limit_names, range_pairs, sym_index
 
 pytestmark = pytest.mark.gpu
 
@@ -37,6 +37,24 @@ def test_gpu_fast_matches_reference_fixtures(name):
     dm = DistMatrix(n + 1)
     FastPairwiseAlign(FastParams.from_dict(g["fast_params"])).pairwiseAlign(aln, dm, *g["range"])
     assert same_bits(dm.getElements(), g["elements"]), f"{np.count_nonzero(dm.getElements() != g['elements'])} differ"
+
+
+@pytest.mark.parametrize("name", quick_limit_names())
+def test_gpu_fast_at_the_length_limit(ctx, oracle_mod, name):
+    """The quick path at its 8191-residue limit (protein ktup 1, DNA ktup 2: an
+    8191-residue sequence, a mutated copy and a fragment), against the
+    DistMatrix the unmodified FastPairwiseAlign filled, bit for bit, and the
+    oracle's per-pair score, fragment count and partial flag."""
+    from clustalw_gb300.native import FastParams
+
+    g = load_fast_golden(name)
+    n = len(g["seqs"])
+    assert max(len(s) for s in g["seqs"]) == 8191
+    ctx.upload_seqs(g["seqs"])
+    el = np.zeros_like(g["elements"])
+    ctx.fast_pairwise_align(FastParams.from_dict(g["fast_params"]), *g["range"], el, n + 1)
+    assert same_bits(el, g["elements"]), f"{np.count_nonzero(el != g['elements'])} differ"
+    check(ctx, oracle_mod, g["seqs"], g["fast_params"])
 
 
 def check(ctx, oracle_mod, seqs, fp, pairs=None):

@@ -5,7 +5,8 @@ Myers-Miller score, identity and match counts)."""
 import numpy as np
 import pytest
 
-from conftest import big_golden_names, golden_names, load_big_extra, load_big_golden, load_golden, range_pairs
+from conftest import (big_golden_names, golden_names, load_big_extra, load_big_golden, load_golden,
+                      pw_variant_names, range_pairs)
 
 pytestmark = pytest.mark.gpu
 
@@ -51,6 +52,30 @@ def test_pair_stats_vs_oracle(ctx, oracle_mod, name):
     for f in STAT_FIELDS:
         bad = np.nonzero(st[f] != want[f])[0]
         assert len(bad) == 0, f"{name}.{f}: {len(bad)} pairs differ, e.g. pair {pairs[bad[0]]}: gpu {st[f][bad[0]]} oracle {want[f][bad[0]]}"
+
+
+@pytest.mark.parametrize("name", pw_variant_names())
+def test_distmatrix_other_matrices_and_gap_penalties(ctx, oracle_mod, name):
+    """The reference's DistMatrix under the BLOSUM, PAM and identity pairwise
+    matrices and non-default gap penalties (protein and DNA, one DNA set with
+    gap extension 0), read as FullPairwiseAlign.cpp:69-94, 129-148 read them:
+    bit-exact through the range call, and every per-pair intermediate equals
+    the oracle's. These stress the shifted E/F carry (gap open + extension)
+    and the int16 score profile with other matrix ranges."""
+    g = load_golden(name)
+    setup(ctx, g)
+    n = len(g["seqs"])
+    elements = np.zeros_like(g["elements"])
+    ctx.pairwise_align(*g["range"], elements, n + 1)
+    bad = np.nonzero(elements != g["elements"])[0]
+    assert len(bad) == 0, f"{name}: {len(bad)} of {len(elements)} entries differ, first {bad[:5]}"
+    pairs = range_pairs(n, *g["range"])
+    dist, st = ctx.align_pairs(pairs, stats=True)
+    want = oracle_mod.align_pairs(g["seqs"], g["matrix"], g["params"], pairs)
+    assert np.array_equal(dist, want["dist"])
+    for f in STAT_FIELDS:
+        bad = np.nonzero(st[f] != want[f])[0]
+        assert len(bad) == 0, f"{name}.{f}: pair {pairs[bad[0]]} gpu {st[f][bad[0]]} oracle {want[f][bad[0]]}"
 
 
 def test_plain_form_matches_batched(ctx):
