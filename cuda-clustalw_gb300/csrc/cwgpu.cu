@@ -2,9 +2,12 @@
 // ordering, persistent graph-captured launch, plain one-launch-per-pair form.
 //
 // Device layout in HBM (all resident for the life of the context):
-//   codes   int8 residues remapped to the K codes that occur, every sequence
-//           starting at a 16-byte boundary
-//   offs    int64 start of each sequence in `codes`
+//   codes   int8 residues remapped to the K codes that occur: guard bytes, then
+//           per sequence its codes and their reversed copy, each starting at a
+//           16-byte boundary, then guard bytes (cwgpu_layout.h)
+//   poffs   int64 start of each sequence's forward copy in `codes`
+//   offs    int64 start of each sequence in the packed original codes (the
+//           quick path uploads those itself)
 //   lens    int32 sequence lengths n (getSeqLength)
 //   nres    int32 residues that are not gapPos1/gapPos2 (len1/len2 of :100-127)
 //   go_tab  int32 gap-open penalty per min(n, m) (FullPairwiseAlign.cpp:129-146)
@@ -25,6 +28,7 @@
 #include "cwgpu.h"
 #include "cwgpu_context.h"
 #include "cwgpu_device.cuh"
+#include "cwgpu_layout.h"
 #include "cwgpu_ranges.h"
 
 namespace {
@@ -35,9 +39,12 @@ constexpr int kCounterWords = 8;   // cwgpu_context::d_counter
 // RS = rows per lane of every sweep: cwgpu::kR for the long-pair kernel,
 // cwgpu::kRShort for pairs whose first sequence has at most
 // cwgpu_tuning::short_rows residues (128 by default: one 4-row stripe).
-// Separate kernels keep the long-pair code exactly as tuned.
+// Separate kernels keep the long-pair code exactly as tuned. Both are held to
+// 5 CTAs (20 warps) per SM, i.e. 96 registers: measured faster than the 113
+// registers and 4 CTAs per SM the compiler picks for the long-pair kernel
+// unbounded (1000 x 1523 protein family, 200 sequences: 110.3 vs 114.7 ms).
 template <int RS>
-__global__ void __launch_bounds__(kWarpsPerBlock * 32, RS == cwgpu::kR ? 0 : 5)
+__global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
     k_pairwise(cwgpu::PairArgs g, long long single) {
     __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
     extern __shared__ __align__(16) uint16_t region_all[];
@@ -224,7 +231,7 @@ cwgpu::PairArgs make_args(cwgpu_context* ctx, const int32_t* d_pairs, const int3
                           float* d_dist, cwgpu_pair_stats* d_stats) {
     cwgpu::PairArgs g;
     g.codes = ctx->d_codes;
-    g.offs = ctx->d_offs;
+    g.offs = ctx->d_poffs;
     g.lens = ctx->d_lens;
     g.nres = ctx->d_nres;
     g.pairs = d_pairs;
@@ -444,6 +451,7 @@ void cwgpu_destroy(cwgpu_context* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     dfree(ctx->d_codes);
+    dfree(ctx->d_poffs);
     dfree(ctx->d_offs);
     dfree(ctx->d_lens);
     dfree(ctx->d_nres);
@@ -523,19 +531,22 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
         code_of[0] = 0;
         K = 1;
     }
-    std::vector<int8_t> dense(packed.size(), 0);
-    for (int s = 0; s < nseqs; ++s)
-        for (int i = 0; i < lens[s]; ++i) dense[doffs[s] + i] = (int8_t)dense_of[codes[offsets[s] + i]];
+    std::vector<int8_t> dense;
+    std::vector<int64_t> poffs;
+    cwgpu::build_layout(
+        nseqs, lens, [&](int s, int i) { return (int8_t)dense_of[codes[offsets[s] + i]]; }, dense, poffs);
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
     ctx->has_seqs = false;
-    CW_CUDA(ctx, grow(ctx->d_codes, ctx->cap_codes, (int64_t)packed.size()));
-    if (nseqs > ctx->cap_seqs || !ctx->d_offs || !ctx->d_lens || !ctx->d_nres) {
-        int64_t c1 = 0, c2 = 0, c3 = 0;
+    CW_CUDA(ctx, grow(ctx->d_codes, ctx->cap_codes, (int64_t)dense.size()));
+    if (nseqs > ctx->cap_seqs || !ctx->d_offs || !ctx->d_poffs || !ctx->d_lens || !ctx->d_nres) {
+        int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
         dfree(ctx->d_offs);
+        dfree(ctx->d_poffs);
         dfree(ctx->d_lens);
         dfree(ctx->d_nres);
         ctx->cap_seqs = 0;
         CW_CUDA(ctx, grow(ctx->d_offs, c1, nseqs));
+        CW_CUDA(ctx, grow(ctx->d_poffs, c4, nseqs));
         CW_CUDA(ctx, grow(ctx->d_lens, c2, nseqs));
         CW_CUDA(ctx, grow(ctx->d_nres, c3, nseqs));
         ctx->cap_seqs = c1;
@@ -543,6 +554,7 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     CW_CUDA(ctx, cudaMemcpy(ctx->d_codes, dense.data(), dense.size(), cudaMemcpyHostToDevice));
     if (nseqs) {
         CW_CUDA(ctx, cudaMemcpy(ctx->d_offs, doffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
+        CW_CUDA(ctx, cudaMemcpy(ctx->d_poffs, poffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
         CW_CUDA(ctx, cudaMemcpy(ctx->d_lens, lens, sizeof(int32_t) * nseqs, cudaMemcpyHostToDevice));
     }
     ctx->nseqs = nseqs;

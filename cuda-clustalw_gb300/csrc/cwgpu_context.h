@@ -32,8 +32,9 @@ struct cwgpu_context {
     int code_of[CWGPU_NUMRES];       // dense index -> original code
     int tiny_m = 32, tiny_n = 16;    // Myers-Miller frames solved one per lane
     int short_rows = 128;            // pairs with a first sequence this short: short-pair kernel
-    int8_t* d_codes = nullptr;
-    int64_t* d_offs = nullptr;
+    int8_t* d_codes = nullptr;   // pair kernels' layout (cwgpu_layout.h): guards, forward and reversed copies
+    int64_t* d_poffs = nullptr;  // forward copy of each sequence in d_codes
+    int64_t* d_offs = nullptr;   // each sequence in host_codes (the quick path's upload of it)
     int32_t* d_lens = nullptr;
     int32_t* d_nres = nullptr;
     int32_t* d_matrix = nullptr;

@@ -40,6 +40,7 @@
 #include <stdint.h>
 
 #include "cwgpu.h"
+#include "cwgpu_layout.h"
 
 namespace cwgpu {
 
@@ -56,9 +57,11 @@ __host__ __device__ constexpr int warp_region_bytes(int K) {
     return (K * 32 * kR * 2 > kTinyWords * 4) ? K * 32 * kR * 2 : kTinyWords * 4;
 }
 
-// One rectangular sweep. Row r (0-based) uses residue rseq[r * rdir]; column c
-// (1-based) uses residue cseq[(c - 1) * cdir]. Closed-form boundaries, which
-// is what every sweep of the reference uses:
+// One rectangular sweep. Row r (0-based) uses residue rseq[r]; column c
+// (1-based) uses residue cseq[c - 1]. Sweeps that run backwards over a
+// sequence read its reversed copy, so every sweep reads its residues in
+// ascending address order. cseq[-kGuard .. cols + kGuard) must be readable.
+// Closed-form boundaries, which is what every sweep of the reference uses:
 //   H(-1, c) = ht0 - c*hts        E(-1, c) = H(-1, c) - eo      (c >= 1)
 //   H(r, 0)  = hl0 - (r+1)*hls    F(r, 0)  = H(r, 0) - fo
 //   H(-1, 0) = 0
@@ -68,7 +71,6 @@ struct Task {
     const int8_t* rseq;
     const int8_t* cseq;
     int2* buf;
-    int rdir, cdir;
     int rows, cols;
     int ht0, hts, eo;
     int hl0, hls, fo;
@@ -98,9 +100,19 @@ struct SweepState {
     int rm[R];  // tracked maximum per row
     int rc[R];  // its first column
     int diag;   // H of the row above the lane's first row, column c-1
-    int hout, eout, thr, bnext;
+    int hout, eout, thr;
     int ch, ce, nh, ne;  // boundary chunks: current and next W columns
 };
+
+// Residue load. NC: through the read-only data path (codes written before the
+// kernel started); otherwise a plain load (codes the kernel itself wrote).
+template <bool NC>
+__device__ __forceinline__ int ldres(const int8_t* p) {
+    if constexpr (NC)
+        return (int)__ldg(p);
+    else
+        return (int)*p;
+}
 
 __device__ __forceinline__ void unpack2(unsigned w, int& lo, int& hi) {
     lo = (int)(int16_t)(w & 0xffffu);
@@ -153,20 +165,26 @@ __device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, c
     }
 }
 
-// The steps of one stripe. Lane 0 of the segment takes the row above from
-// the chunk registers (W columns per lane-wide load: the previous stripe's last
-// row, or the closed-form top boundary for the first stripe). PARTIAL: some
-// rows of the stripe are past the task's last row; they pass the row above
-// through so the segment's last used lane still emits the last real row. One
-// loop body per (MODE, PARTIAL) keeps the hot code small enough for the
-// instruction cache; lanes outside their column range skip the body.
-template <int R, int W, int MODE, bool PARTIAL>
+// The steps of one stripe. Lane sl processes column c = t - sl + 1 at step t.
+// Lane 0 of the segment takes the row above from the chunk registers (W columns
+// per lane-wide load: the previous stripe's last row, or the closed-form top
+// boundary for the first stripe). PARTIAL: some rows of the stripe are past the
+// task's last row; they pass the row above through so the segment's last used
+// lane still emits the last real row. One loop body per (MODE, PARTIAL) keeps
+// the hot code small enough for the instruction cache (unrolling the step loop
+// made it slower for that reason); lanes outside their column range skip the
+// body. The next step's residue is loaded one step ahead from the lane's own
+// pointer, without clamping (the layout's guard bytes make the reads of fill
+// and drain steps safe; those residues are never used).
+template <int R, int W, int MODE, bool PARTIAL, bool NC>
 __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T, SweepState<R>& S, int sl,
                                            int nvalid, bool writer, int ge, int goe, int thresh,
                                            const uint16_t* prof_lane) {
-    const int cmax = T.cols - 1;
+    const unsigned ucols = (unsigned)T.cols;
+    const int8_t* cp = T.cseq - sl;  // residue of step t: cp[t]
+    int2* wp = T.buf + 1 - sl;       // boundary-row entry of step t: wp[t]
+    int bnext = ldres<NC>(cp);
     for (int t = 0; t < nsteps; ++t) {
-        const int c = t - sl + 1;
         int hin = __shfl_up_sync(kFull, S.hout, 1, W);
         int ein = __shfl_up_sync(kFull, S.eout, 1, W);
         const int idx = t & (W - 1);
@@ -189,9 +207,9 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
                 S.ne = v.y;
             }
         }
-        const int b = S.bnext;
-        S.bnext = (int)__ldg(T.cseq + min(max(c, 0), cmax) * T.cdir);  // next step's column, clamped in range
-        if ((unsigned)(c - 1) < (unsigned)T.cols) {
+        const int b = bnext;
+        bnext = ldres<NC>(cp + t + 1);
+        if ((unsigned)(t - sl) < ucols) {
             int sc[R];
             load_scores<R>(prof_lane + b * (32 * R), sc);
             int hup = hin, eup = ein, d = S.diag;
@@ -228,6 +246,7 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
                 if ((R & 1) == 0) sm = max(sm, hs[R - 1]);
                 if (MODE == MODE_LOCAL_REV) sm = min(sm, thresh);
                 if (sm >= S.thr) {
+                    const int c = t - sl + 1;
 #pragma unroll
                     for (int k = 0; k < R; ++k) {
                         const int hv = (MODE == MODE_LOCAL_REV) ? min(hs[k], thresh) : hs[k];
@@ -239,7 +258,7 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
                     S.thr = sm;
                 }
             }
-            if (writer) T.buf[c] = make_int2(hup, eup);
+            if (writer) wp[t] = make_int2(hup, eup);
         }
     }
 }
@@ -253,7 +272,7 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
 // stripe that reached thresh. Tracking runs on the per-step maximum of the
 // lane's rows; only when it reaches the lane's running maximum are the rows
 // examined one by one.
-template <int R, int W, int MODE>
+template <int R, int W, int MODE, bool NC = true>
 __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, Best& best) {
     const int lane = threadIdx.x & 31;
     const int sl = lane & (W - 1);
@@ -280,7 +299,7 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, B
 
         int a[R];
 #pragma unroll
-        for (int k = 0; k < R; ++k) a[k] = (k < nvalid) ? (int)__ldg(T.rseq + (lrow0 + k) * T.rdir) : 0;
+        for (int k = 0; k < R; ++k) a[k] = (k < nvalid) ? ldres<NC>(T.rseq + lrow0 + k) : 0;
         __syncwarp();  // previous users of the shared region are done
         build_profile<R>(X.region, X.smat, a, lane, X.K);
         __syncwarp();  // previous stripe's buf writes visible to the whole segment
@@ -297,7 +316,6 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, B
         S.hout = 0;
         S.eout = 0;
         S.thr = gbest + 1;
-        S.bnext = (int)__ldg(T.cseq);  // column 1, used by lane 0 at step 0
         const bool first = (s == 0);
         if (first) {
             S.ch = T.ht0 - (1 + sl) * T.hts;
@@ -318,9 +336,9 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, B
             }
         }
         if (full)
-            run_stripe<R, W, MODE, false>(nsteps_max, first, T, S, sl, nvalid, writer, ge, goe, thresh, prof_lane);
+            run_stripe<R, W, MODE, false, NC>(nsteps_max, first, T, S, sl, nvalid, writer, ge, goe, thresh, prof_lane);
         else
-            run_stripe<R, W, MODE, true>(nsteps_max, first, T, S, sl, nvalid, writer, ge, goe, thresh, prof_lane);
+            run_stripe<R, W, MODE, true, NC>(nsteps_max, first, T, S, sl, nvalid, writer, ge, goe, thresh, prof_lane);
 
         if (MODE != MODE_GLOBAL) {
             // Earliest row of this lane holding the lane's maximum (rows ascend with k).
@@ -352,6 +370,7 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, B
 // shared scratch (word j*32 + lane, conflict-free), the frame stack in local
 // memory. Returns the frame's score; adds identities, matches and diff()
 // inner-loop iterations.
+template <bool NC>
 static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int tbf0, int tef0, int go,
                        int ge, const Env& X, int* scratch, int& ident, int& matches, long long& cells) {
     const int lane = threadIdx.x & 31;
@@ -383,9 +402,9 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
                 const int hh0 = -(te + ge) - (tb + ge * N);
                 if (hh0 > midh) midh = hh0;
                 int midj = 0;
-                const int* row = X.smat + 32 * (int)__ldg(s1 + A);
+                const int* row = X.smat + 32 * ldres<NC>(s1 + A);
                 for (int j = 1; j <= N; ++j) {
-                    const int hh = row[__ldg(s2 + B + j - 1)] - (N - j > 0 ? te + ge * (N - j) : 0) -
+                    const int hh = row[ldres<NC>(s2 + B + j - 1)] - (N - j > 0 ? te + ge * (N - j) : 0) -
                                    (j - 1 > 0 ? tb + ge * (j - 1) : 0);
                     if (hh > midh) {
                         midh = hh;
@@ -394,7 +413,7 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
                 }
                 if (midj > 0) {
                     ++matches;
-                    const int ra = __ldg(s1 + A), rb = __ldg(s2 + B + midj - 1);
+                    const int ra = ldres<NC>(s1 + A), rb = ldres<NC>(s2 + B + midj - 1);
                     if (ra != X.gp1 && rb != X.gp2 && ra == rb) ++ident;
                 }
             }
@@ -410,7 +429,7 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
             }
             t = -tb;
             for (int i = 1; i <= midi; ++i) {
-                const int* row = X.smat + 32 * (int)__ldg(s1 + A + i - 1);
+                const int* row = X.smat + 32 * ldres<NC>(s1 + A + i - 1);
                 int s = TI(HH, 0);
                 int hh = t = t - ge;
                 TI(HH, 0) = hh;
@@ -418,7 +437,7 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
                 for (int j = 1; j <= N; ++j) {
                     f = max(f - ge, hh - go - ge);
                     const int e = max(TI(DD, j) - ge, TI(HH, j) - go - ge);
-                    hh = max(max(s + row[__ldg(s2 + B + j - 1)], f), e);
+                    hh = max(max(s + row[ldres<NC>(s2 + B + j - 1)], f), e);
                     s = TI(HH, j);
                     TI(HH, j) = hh;
                     TI(DD, j) = e;
@@ -434,7 +453,7 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
             }
             t = -te;
             for (int i = M - 1; i >= midi; --i) {
-                const int* row = X.smat + 32 * (int)__ldg(s1 + A + i);
+                const int* row = X.smat + 32 * ldres<NC>(s1 + A + i);
                 int s = TI(RR, N);
                 int hh = t = t - ge;
                 TI(RR, N) = hh;
@@ -442,7 +461,7 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
                 for (int j = N - 1; j >= 0; --j) {
                     f = max(f - ge, hh - go - ge);
                     const int e = max(TI(SS, j) - ge, TI(RR, j) - go - ge);
-                    hh = max(max(s + row[__ldg(s2 + B + j)], f), e);
+                    hh = max(max(s + row[ldres<NC>(s2 + B + j)], f), e);
                     s = TI(RR, j);
                     TI(RR, j) = hh;
                     TI(SS, j) = e;
@@ -498,11 +517,12 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
 // match counts are sums over the M == 1 leaves, so the traversal order is
 // free; the top frame's score is diff()'s return value. tb/te are always 0 or
 // gapOpen, kept as flags. s1/s2 are 0-based: the reference's 1-based residue
-// seq1[A + i] is s1[A + i - 1].
-template <int RS>
-static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int B0, int M0, int N0, int go, int ge,
-                         int2* bufA, int2* bufB, const Env& X, int& mm_score, int& n_ident, int& n_match,
-                         long long& cells) {
+// seq1[A + i] is s1[A + i - 1]. s1r/s2r are the reversed copies of the n- and
+// m-residue sequences (s1r[i] = s1[n - 1 - i]), which the reverse halves read.
+template <int RS, bool NC = true>
+static __device__ void mm_align(const int8_t* s1, const int8_t* s1r, int n, const int8_t* s2, const int8_t* s2r, int m,
+                                int A0, int B0, int M0, int N0, int go, int ge, int2* bufA, int2* bufB, const Env& X,
+                                int& mm_score, int& n_ident, int& n_match, long long& cells) {
     const int lane = threadIdx.x & 31;
     constexpr int NMASK = (1 << 29) - 1;
     const int goe = go + ge;
@@ -527,7 +547,7 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int 
             int li = 0, lm = 0, score = 0;
             long long lc = 0;
             if (lane < nq) {
-                score = lane_mm(s1, s2, qA, qB, qM, qN & NMASK, (qN >> 29) & 1, (qN >> 30) & 1, go, ge, X,
+                score = lane_mm<NC>(s1, s2, qA, qB, qM, qN & NMASK, (qN >> 29) & 1, (qN >> 30) & 1, go, ge, X,
                                 reinterpret_cast<int*>(X.region), li, lm, lc);
             }
             __syncwarp();
@@ -576,10 +596,10 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int 
             int midh = -(tb + ge) - (te + ge * N);
             const int hh0 = -(te + ge) - (tb + ge * N);
             if (hh0 > midh) midh = hh0;
-            const int ra = (int)__ldg(s1 + A);
+            const int ra = ldres<NC>(s1 + A);
             int bv = INT_MIN, bj = 0x7fffffff;
             for (int j = lane + 1; j <= N; j += 32) {
-                const int rb = (int)__ldg(s2 + B + j - 1);
+                const int rb = ldres<NC>(s2 + B + j - 1);
                 const int v = X.smat[ra * 32 + rb] - (N - j > 0 ? te + ge * (N - j) : 0) -
                               (j - 1 > 0 ? tb + ge * (j - 1) : 0);
                 if (v > bv) {
@@ -591,7 +611,7 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int 
             const int wj = (int)__reduce_min_sync(kFull, bv == wv ? (unsigned)bj : 0x7fffffffu);
             if (wv > midh) {
                 midh = wv;
-                const int rb = (int)__ldg(s2 + B + wj - 1);
+                const int rb = ldres<NC>(s2 + B + wj - 1);
                 ++matches;
                 if (ra != X.gp1 && rb != X.gp2 && ra == rb) ++ident;
             }
@@ -606,18 +626,16 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int 
         Task t;
         if (lane < 16) {
             t.rseq = s1 + A;
-            t.rdir = 1;
             t.cseq = s2 + B;
-            t.cdir = 1;
             t.rows = midi;
             t.ht0 = -tb;
             t.hl0 = -tb;
             t.buf = bufA;
         } else {
-            t.rseq = s1 + A + M - 1;
-            t.rdir = -1;
-            t.cseq = s2 + B + N - 1;
-            t.cdir = -1;
+            // rows A+M-1 down to A+midi and columns B+N-1 down to B, read in
+            // ascending order from the reversed copies
+            t.rseq = s1r + (n - A - M);
+            t.cseq = s2r + (m - B - N);
             t.rows = M - midi;
             t.ht0 = -te;
             t.hl0 = -te;
@@ -629,7 +647,7 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s2, int A0, int 
         t.hls = ge;
         t.fo = go;
         Best unused;
-        sweep<RS, 16, MODE_GLOBAL>(t, go, ge, 0, X, unused);
+        sweep<RS, 16, MODE_GLOBAL, NC>(t, go, ge, 0, X, unused);
 
         // Midpoint scans (:570-593). Scan 1 keeps the first j reaching the
         // maximum of HH+RR, replaced by the last tied j with HH!=DD && RR==SS;
@@ -754,18 +772,21 @@ struct PairArgs {
 // inner-loop iterations the reference executes) to acc[0..2]. RS = rows per
 // lane in every sweep: any RS gives the same results; kRShort needs fewer
 // warp steps when n <= 128 (one stripe, lanes of 4 rows instead of
-// half-empty lanes of 8).
-template <int RS = kR>
+// half-empty lanes of 8). Each sequence's reversed copy follows it at the
+// next 16-byte boundary (cwgpu_layout.h), and kGuard readable bytes surround both.
+__device__ __forceinline__ const int8_t* rev_of(const int8_t* s, int len) { return s + rev_offset(len); }
+
+template <int RS = kR, bool NC = true>
 static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int m, int len1, int len2, int go, int ge,
                            int2* bufA, int2* bufB, const Env& X, cwgpu_pair_stats& st, unsigned long long (&acc)[3]) {
+    const int8_t* s1r = rev_of(s1, n);
+    const int8_t* s2r = rev_of(s2, m);
     st = cwgpu_pair_stats{0, 0, 0, 0, 0, 0, 0, 0};
     if (n <= 0 || m <= 0) return 1.0f;
     // forwardPass
     Task t;
     t.rseq = s1;
-    t.rdir = 1;
     t.cseq = s2;
-    t.cdir = 1;
     t.rows = n;
     t.cols = m;
     t.ht0 = 0;
@@ -776,7 +797,7 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
     t.fo = go;
     t.buf = bufA;
     Best fb;
-    sweep<RS, 32, MODE_LOCAL_FWD>(t, go, ge, 0, X, fb);
+    sweep<RS, 32, MODE_LOCAL_FWD, NC>(t, go, ge, 0, X, fb);
     const int max_score = fb.val;
     const int se1 = max_score > 0 ? (int)(fb.key >> 16) + 1 : 0;
     const int se2 = max_score > 0 ? (int)(fb.key & 0xffffu) : 0;
@@ -785,10 +806,8 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
     int sb1 = 1, sb2 = 1;
     if (se1 > 0) {
         Task r;
-        r.rseq = s1 + se1 - 1;
-        r.rdir = -1;
-        r.cseq = s2 + se2 - 1;
-        r.cdir = -1;
+        r.rseq = s1r + (n - se1);  // rows se1-1 .. 0 of s1
+        r.cseq = s2r + (m - se2);  // columns se2 .. 1
         r.rows = se1;
         r.cols = se2;
         r.ht0 = -1;
@@ -799,7 +818,7 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
         r.fo = 0;
         r.buf = bufA;
         Best rb;
-        sweep<RS, 32, MODE_LOCAL_REV>(r, go, ge, max_score, X, rb);
+        sweep<RS, 32, MODE_LOCAL_REV, NC>(r, go, ge, max_score, X, rb);
         if (rb.val > 0) {
             sb1 = se1 - (int)(rb.key >> 16);
             sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
@@ -815,8 +834,8 @@ static __device__ float align_one(const int8_t* s1, int n, const int8_t* s2, int
     // diff + tracePath
     int mm = 0, ident = 0, matches = 0;
     long long dcells = 0;
-    mm_align<RS>(s1, s2, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, bufA, bufB, X, mm, ident, matches,
-             dcells);
+    mm_align<RS, NC>(s1, s1r, n, s2, s2r, m, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, bufA, bufB, X, mm,
+                 ident, matches, dcells);
     acc[2] += (unsigned long long)dcells;
 
     // distance (:170-181), float arithmetic with IEEE rounding.

@@ -6,8 +6,8 @@
 // start-up, or callers between a memory-pool reservation and its use. They
 // can still hand over device buffers they already own. This entry point runs
 // the same pair kernel as cwgpu_align_pairs, but every byte of working memory
-// it needs (per-warp boundary rows, the queue head, the cell counters, the
-// status words and the gap-open table) lives in one file-scope static device
+// it needs (per-warp boundary rows and residue copies, the queue head, the cell
+// counters, the status words and the gap-open table) lives in one file-scope static device
 // array, g_noalloc_scratch, of CWGPU_NOALLOC_SCRATCH_BYTES (16 MiB). Every GPU that
 // loads this library holds that array until the process exits.
 //
@@ -28,6 +28,7 @@
 
 #include "cwgpu.h"
 #include "cwgpu_device.cuh"
+#include "cwgpu_layout.h"
 
 namespace {
 
@@ -63,13 +64,23 @@ __device__ __forceinline__ int* na_status(unsigned char* scratch, int which) {
     return reinterpret_cast<int*>(scratch + 4 * sizeof(unsigned long long)) + which;
 }
 
+// Bytes of one warp slot: the two boundary rows, then the pair's residues in
+// the pair kernels' layout (guards, forward and reversed copy of each
+// sequence; cwgpu_layout.h), rounded to 256.
+__host__ __device__ inline size_t na_slot_bytes(int max_len) {
+    const size_t rows = 2 * (size_t)(max_len + 1) * sizeof(int2);
+    const size_t codes = 2 * (size_t)cwgpu::kGuard + 4 * (size_t)cwgpu::rev_offset(max_len);
+    return (rows + codes + 255) & ~(size_t)255;
+}
+
 // One pair (FullPairwiseAlign.cpp:112-183) with device-side input checks: a
 // pair index, a negative sequence offset, a length above max_len or a residue
 // code outside [0, 31] sets the input status word and the pair is skipped. The
 // residue counts len1/len2 of :100-127 are counted here instead of being
-// uploaded.
+// uploaded. The two sequences are copied into the slot (forward and reversed)
+// and read back from there with plain loads, since the kernel wrote them.
 __device__ void na_align_pair(const NaArgs& a, long long q, const cwgpu::Env& X, int2* bufA, int2* bufB,
-                              unsigned long long (&acc)[3]) {
+                              int8_t* slot_codes, unsigned long long (&acc)[3]) {
     const int lane = threadIdx.x & 31;
     int* status = na_status(a.scratch, kNaStatusInput);
     const int32_t* go_table = reinterpret_cast<const int32_t*>(a.scratch + kNaCtrlBytes);
@@ -101,8 +112,25 @@ __device__ void na_align_pair(const NaArgs& a, long long q, const cwgpu::Env& X,
         return;
     }
     const int len1 = __reduce_add_sync(cwgpu::kFull, r1), len2 = __reduce_add_sync(cwgpu::kFull, r2);
+    int8_t* p1 = slot_codes + cwgpu::kGuard;
+    int8_t* p1r = p1 + cwgpu::rev_offset(n);
+    int8_t* p2 = p1r + cwgpu::rev_offset(n);
+    int8_t* p2r = p2 + cwgpu::rev_offset(m);
+    __syncwarp();  // the previous pair's reads of the slot are done
+    for (int i = lane; i < n; i += 32) {
+        const int8_t c = s1[i];
+        p1[i] = c;
+        p1r[n - 1 - i] = c;
+    }
+    for (int i = lane; i < m; i += 32) {
+        const int8_t c = s2[i];
+        p2[i] = c;
+        p2r[m - 1 - i] = c;
+    }
+    __syncwarp();  // copies visible to the whole warp
     cwgpu_pair_stats st;
-    const float dist = cwgpu::align_one(s1, n, s2, m, len1, len2, go_table[min(n, m)], a.ge, bufA, bufB, X, st, acc);
+    const float dist = cwgpu::align_one<cwgpu::kR, false>(p1, n, p2, m, len1, len2, go_table[min(n, m)], a.ge, bufA,
+                                                          bufB, X, st, acc);
     if (lane == 0) {
         a.dist[q] = dist;
         if (a.stats) a.stats[q] = st;
@@ -138,16 +166,17 @@ __global__ void __launch_bounds__(kNaWarpsPerBlock * 32) k_pairwise_noalloc(NaAr
     X.tiny_n = cwgpu::kTinyMaxN;
     unsigned long long* ctrl = reinterpret_cast<unsigned long long*>(a.scratch);
     X.err = na_status(a.scratch, kNaStatusLimit);
-    int2* rows = reinterpret_cast<int2*>(a.scratch + kNaRowsOffset);
-    int2* bufA = rows + (size_t)slot * 2 * (a.max_len + 1);
+    unsigned char* my_slot = a.scratch + kNaRowsOffset + (size_t)slot * na_slot_bytes(a.max_len);
+    int2* bufA = reinterpret_cast<int2*>(my_slot);
     int2* bufB = bufA + (a.max_len + 1);
+    int8_t* slot_codes = reinterpret_cast<int8_t*>(bufB + (a.max_len + 1));
     unsigned long long acc[3] = {0, 0, 0};
     for (;;) {
         unsigned long long k = 0;
         if (lane == 0) k = atomicAdd(ctrl, 1ULL);
         k = __shfl_sync(cwgpu::kFull, k, 0);
         if (k >= (unsigned long long)a.npairs) break;
-        na_align_pair(a, (long long)k, X, bufA, bufB, acc);
+        na_align_pair(a, (long long)k, X, bufA, bufB, slot_codes, acc);
     }
     if (lane == 0 && (acc[0] | acc[1] | acc[2])) {
         atomicAdd(ctrl + 1, acc[0]);
@@ -234,8 +263,7 @@ extern "C" int cwgpu_align_pairs_noalloc(const int8_t* d_codes, const int64_t* d
         cwgpu_gap_penalties(params, L, L, &table[L], &unused);
     }
 
-    const size_t row_bytes = 2 * (size_t)(max_len + 1) * sizeof(int2);
-    const long long slots = (long long)((kNaScratchBytes - kNaRowsOffset) / row_bytes);
+    const long long slots = (long long)((kNaScratchBytes - kNaRowsOffset) / na_slot_bytes(max_len));
     long long grid = slots / kNaWarpsPerBlock;
     const long long full = (long long)d->sm_count * d->blocks_per_sm;
     if (grid > full) grid = full;

@@ -37,6 +37,7 @@
 
 #include "cwgpu.h"
 #include "cwgpu_device.cuh"
+#include "cwgpu_layout.h"
 
 namespace {
 
@@ -71,7 +72,7 @@ struct JobsArgs {
     int tiny_m, tiny_n;
 };
 
-__global__ void __launch_bounds__(kSrvWarpsPerBlock * 32) k_pairwise_jobs(JobsArgs a) {
+__global__ void __launch_bounds__(kSrvWarpsPerBlock * 32, 5) k_pairwise_jobs(JobsArgs a) {
     __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
     extern __shared__ __align__(16) uint16_t srv_region[];
     for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = a.matrix[i];
@@ -171,7 +172,7 @@ struct Job {
     int want_stats = 0;
     int64_t npairs = 0;
     int lmax = 0;
-    std::vector<int8_t> codes;  // dense codes, each sequence 16-byte aligned
+    std::vector<int8_t> codes;  // dense codes in the pair kernels' layout (cwgpu_layout.h)
     std::vector<int64_t> offs;
     std::vector<int32_t> lens, nres;
     int64_t cells_nm = 0;
@@ -260,19 +261,14 @@ void remap_job(cwgpu_server* s, Job* j, const int8_t* codes, const int64_t* offs
                 s->matrix_dirty = true;
             }
         }
-    int64_t total = 0;
-    j->offs.resize(j->nseqs);
-    for (int q = 0; q < j->nseqs; ++q) {
-        j->offs[q] = total;
-        total += (j->lens[q] + 15) & ~15;
-    }
-    j->codes.assign((size_t)std::max<int64_t>(total, 16), 0);
+    cwgpu::build_layout(
+        j->nseqs, j->lens.data(), [&](int q, int i) { return (int8_t)s->dense_of[codes[offsets[q] + i]]; }, j->codes,
+        j->offs);
     j->nres.resize(j->nseqs);
     for (int q = 0; q < j->nseqs; ++q) {
         int r = 0;
         for (int i = 0; i < j->lens[q]; ++i) {
             const int c = codes[offsets[q] + i];
-            j->codes[j->offs[q] + i] = (int8_t)s->dense_of[c];
             r += (c != s->params.gap_pos1 && c != s->params.gap_pos2);
         }
         j->nres[q] = r;

@@ -47,10 +47,11 @@ def load_golden(name):
 def golden_names():
     """Full-pairwise fixtures with the default parameters (guide-tree fixtures
     start with nj_, quick k-tuple fixtures with fast_ or quicklimit_, other
-    pairwise parameters with pwparams_, compact full-size ones with big_)."""
+    pairwise parameters with pwparams_, compact full-size ones with big_, the
+    benchmark workloads' whole-set hashes with bench_)."""
     return sorted(f[:-4] for f in os.listdir(GOLDEN)
                   if f.endswith(".npz")
-                  and not f.startswith(("nj_", "fast_", "quicklimit_", "quickparams_", "pwparams_", "big_")))
+                  and not f.startswith(("nj_", "fast_", "quicklimit_", "quickparams_", "pwparams_", "big_", "bench_")))
 
 
 def pw_variant_names():
