@@ -23,6 +23,12 @@ divided by the time of the step.
              kernel (device-resident and through the C ABI) beside the oracle
   quick      FastPairwiseAlign (k-tuple distances) on the same sequences:
              GPU kernel beside the oracle on all host threads
+  few_pairs  launches with few long pairs (the reference's 100_1523 set whole
+             and as a one-column call, 20 and 6 sequences of ~3000 residues):
+             the default dispatch (one CTA per pair below a threshold) beside
+             one warp per pair
+  reference_shaped  the reference fork's launch shape (128 pairs per launch,
+             4 streams) with these kernels, beside the batched form
 --impl reference times the reference CPU algorithm (the oracle port; the
 reference's own build is not available on the GPU host) on all host threads.
 """
@@ -73,6 +79,8 @@ def parse_args():
     ap.add_argument("--no-serve", action="store_true")
     ap.add_argument("--no-tree", action="store_true", help="skip the guide-tree leg")
     ap.add_argument("--no-quick", action="store_true", help="skip the quick k-tuple distance leg")
+    ap.add_argument("--no-few", action="store_true",
+                    help="skip the few-pair launches and the reference-shaped comparator")
     ap.add_argument("--autotune", action="store_true", help="pick the tiny-frame thresholds for this workload first")
     return ap.parse_args()
 
@@ -258,6 +266,124 @@ def reference_arm(args):
     print(json.dumps(line), flush=True)
 
 
+# ---------------------------------------------------------------- launches with few pairs
+
+
+def _time_plan(plan, stream, steps):
+    import torch
+
+    plan.launch(stream.cuda_stream)
+    torch.cuda.synchronize()
+    ts = []
+    for _ in range(steps):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        plan.launch(stream.cuda_stream)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ts.append(e0.elapsed_time(e1))
+    return statistics.median(ts)
+
+
+def few_pairs_leg(args, device):
+    """Launches with fewer long pairs than the long-pair kernel has warps, each
+    timed (CUDA events, median of the steps) as dispatched by default and with
+    one warp per pair forced (cwgpu_cta_tuning max_pairs 0); both give the same
+    distances. Cases: the reference's own 100-sequence DNA set
+    (test_data/correct/100_1523.fa, stored in tests/golden/fixture_100_1523.npz)
+    whole and as the one-column call sequencesAlignToProfile makes
+    (Clustal.cpp:404-416: pairs (i, 99)), and synthetic protein families of
+    20 and 6 sequences of about 3000 residues."""
+    import torch
+
+    from clustalw_gb300 import load_matrix, native, synth
+
+    z = np.load(os.path.join(REPO, "tests", "golden", "fixture_100_1523.npz"))
+    offs = np.concatenate([[0], np.cumsum(z["lens"])[:-1]])
+    ref_seqs = [z["codes"][o : o + L].astype(np.int8) for o, L in zip(offs, z["lens"])]
+    dna_m, dna_p = load_matrix("dna")
+    prot_m, prot_p = load_matrix("protein")
+    n = len(ref_seqs)
+    cases = [
+        ("reference-100x1523-dna-one-column", ref_seqs, dna_m, dna_p,
+         np.stack([np.arange(n - 1), np.full(n - 1, n - 1)], axis=1).astype(np.int32)),
+        ("reference-100x1523-dna-all", ref_seqs, dna_m, dna_p, synth.all_pairs(n)),
+        ("protein-20x3000", synth.protein_family(20, 3000, args.seed), prot_m, prot_p, synth.all_pairs(20)),
+        ("protein-6x3000", synth.protein_family(6, 3000, args.seed), prot_m, prot_p, synth.all_pairs(6)),
+    ]
+    stream = torch.cuda.Stream()
+    out = {}
+    with native.Context(device) as ctx:
+        for name, seqs, matrix, params, pairs in cases:
+            ctx.set_matrix(matrix)
+            ctx.set_params(params)
+            ctx.upload_seqs(seqs)
+            cells = nm_cells(seqs, pairs)
+            res = {"pairs": int(len(pairs))}
+            dists = []
+            for label, max_pairs in (("default", None), ("one_warp_per_pair", 0)):
+                old = ctx.get_cta_tuning()
+                if max_pairs is not None:
+                    ctx.set_cta_tuning(max_pairs=max_pairs)
+                plan = ctx.plan(pairs)
+                ms = _time_plan(plan, stream, 5)
+                dists.append(plan.results())
+                res[label] = {"gcups": cells / (ms / 1e3) / 1e9, "ms": ms,
+                              "form": "one CTA per pair" if plan.pair_ctas() else "one warp per pair"}
+                plan.close()
+                ctx.set_cta_tuning(*old)
+            if not np.array_equal(dists[0], dists[1]):
+                raise RuntimeError(f"{name}: the two forms disagree")
+            res["default_over_one_warp"] = res["default"]["gcups"] / res["one_warp_per_pair"]["gcups"]
+            out[name] = res
+    return out
+
+
+def ref_shaped_leg(args, seqs, matrix, params, pairs, device, batched_gcups):
+    """The reference fork's launch shape with this project's kernels: 128 pairs
+    per launch, launches round-robin over 4 streams (G/cuda/cudaFullPairwiseAlign.cu:
+    14-20, 977-1036), each stream with its own context (plans of one context
+    share its scratch), on a seeded uniform sample of the workload's pairs.
+    Timed with one warp per pair and with one CTA per pair, next to the
+    batched form's GCUPS on the whole workload."""
+    import torch
+
+    from clustalw_gb300 import native
+
+    rng = np.random.default_rng(args.seed + 77)
+    nchunks = 4 * 12
+    sample = pairs[np.sort(rng.choice(len(pairs), size=min(len(pairs), 128 * nchunks), replace=False))]
+    chunks = [sample[k : k + 128] for k in range(0, len(sample), 128)]
+    res = {"pairs_per_launch": 128, "streams": 4, "sample_pairs": int(len(sample))}
+    for label, max_pairs in (("one_warp_per_pair", 0), ("one_cta_per_pair", 2**31 - 1)):
+        ctxs = [native.Context(device) for _ in range(4)]
+        streams = [torch.cuda.Stream() for _ in range(4)]
+        plans = []
+        for c in ctxs:
+            c.set_cta_tuning(max_pairs=max_pairs)
+            c.set_matrix(matrix)
+            c.set_params(params)
+            c.upload_seqs(seqs)
+        for k, ch in enumerate(chunks):
+            plans.append((ctxs[k % 4].plan(ch), streams[k % 4]))
+        best = float("inf")
+        for rep in range(3):
+            torch.cuda.synchronize()
+            t = time.perf_counter()
+            for pl, st in plans:
+                pl.launch(st.cuda_stream)
+            torch.cuda.synchronize()
+            if rep:
+                best = min(best, time.perf_counter() - t)
+        gcups = nm_cells(seqs, sample) / best / 1e9
+        res[label] = {"gcups": gcups, "batched_over_this": batched_gcups / gcups}
+        for pl, _ in plans:
+            pl.close()
+        for c in ctxs:
+            c.close()
+    return res
+
+
 # ---------------------------------------------------------------- served leg
 
 
@@ -322,6 +448,7 @@ def served_leg(args, matrix, params, device):
         "offered_gcups": sum(cells) / wall / 1e9,
         "capacity_gcups": sum(cells) / burst_s / 1e9,
         "plain_per_job_gcups": c_plain / t_plain / 1e9,
+        "capacity_over_plain_per_job": (sum(cells) / burst_s) / (c_plain / t_plain),
         "plain_sample_jobs": len(sample),
         "rounds": info["rounds"],
         "policy": "least remaining work first; jobs older than 500 ms first, in admission order",
@@ -707,6 +834,9 @@ def ours_arm(args):
                 line["guide_tree"] = guide_tree_leg(args, len(seqs), pairs, dist_out, local, peaks)
             if not args.no_quick:
                 line["quick"] = quick_leg(args, ctx, seqs, pairs, local)
+            if not args.no_few:
+                line["few_pairs"] = few_pairs_leg(args, local)
+                line["reference_shaped"] = ref_shaped_leg(args, seqs, matrix, params, pairs, local, value)
         print(json.dumps(line), flush=True)
     plan.close()
     ctx.close()

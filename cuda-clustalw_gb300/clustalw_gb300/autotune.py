@@ -13,6 +13,11 @@ depend on the knobs, only the time does. Choices are cached per GPU and length
 profile in $XDG_CACHE_HOME/clustalw_gb300/tuning.json. $CLUSTALW_GB300_TUNING
 ("tiny_m,tiny_n,short_rows") overrides both the cache and the search, and is
 applied to every new native.Context.
+
+tune_cta() picks the one-CTA-per-pair knobs (cwgpu_cta_tuning) for a launch
+with few long pairs: it times the whole launch one warp per pair and one CTA
+per pair with 4, 8 and 16 warps, and sets the threshold so that a launch of
+this size takes the faster form.
 """
 import json
 import os
@@ -135,4 +140,34 @@ def tune(ctx, lens, pairs, gpu_name="gpu", target_cells=2e10, candidates=CANDIDA
                 json.dump(cache, f, indent=1)
         except OSError:
             pass
+    return choice, timings
+
+
+CTA_WARPS = [4, 8, 16]
+CTA_MAX_TIMED_PAIRS = 4096  # above this one warp per pair fills the GPU; nothing is timed
+
+
+def tune_cta(ctx, lens, pairs, warps=CTA_WARPS, repeats=2):
+    """Pick cwgpu_cta_tuning (max_pairs, warps, large_rows) for launches of
+    `pairs` on `ctx` (matrix, params and sequences set), apply it and return
+    (choice, {(max_pairs, warps): seconds}). Only the long pairs (first
+    sequence longer than short_rows) can take the CTA form; a launch with more
+    than CTA_MAX_TIMED_PAIRS of them keeps the current knobs untimed."""
+    lens = np.asarray(lens)
+    pairs = np.asarray(pairs).reshape(-1, 2)
+    short_rows = ctx.get_tuning()[2]
+    nlong = int((lens[pairs[:, 0]] > short_rows).sum()) if len(pairs) else 0
+    cur = ctx.get_cta_tuning()
+    if nlong == 0 or nlong > CTA_MAX_TIMED_PAIRS:
+        return cur, {}
+    large = cur[2]
+    timings = {(0, cur[1]): None}
+    ctx.set_cta_tuning(0, cur[1], large)
+    timings[(0, cur[1])] = _time_sample(ctx, pairs, repeats)
+    for w in warps:
+        ctx.set_cta_tuning(nlong, w, large)
+        timings[(nlong, w)] = _time_sample(ctx, pairs, repeats)
+    best = min(timings, key=timings.get)
+    choice = (nlong if best[0] else nlong - 1, best[1], large)
+    ctx.set_cta_tuning(*choice)
     return choice, timings

@@ -99,6 +99,12 @@ class Tuning(ctypes.Structure):
     _fields_ = [("tiny_m", ctypes.c_int32), ("tiny_n", ctypes.c_int32), ("short_rows", ctypes.c_int32)]
 
 
+class CtaTuning(ctypes.Structure):
+    """cwgpu_cta_tuning: when and how long pairs run one CTA per pair."""
+
+    _fields_ = [("max_pairs", ctypes.c_int32), ("warps", ctypes.c_int32), ("large_rows", ctypes.c_int32)]
+
+
 class ServerOpts(ctypes.Structure):
     _fields_ = [
         ("memory_budget_bytes", ctypes.c_int64),
@@ -150,10 +156,14 @@ SIGNATURES = {
     "cwgpu_plan_device_dist": (_vp, [_vp]),
     "cwgpu_plan_cell_counts": (ctypes.c_int, [_vp, _vp]),
     "cwgpu_plan_kernel_count": (ctypes.c_int, [_vp]),
+    "cwgpu_plan_pair_ctas": (ctypes.c_int, [_vp]),
     "cwgpu_plan_destroy": (None, [_vp]),
     "cwgpu_synchronize": (ctypes.c_int, [_vp]),
     "cwgpu_set_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
     "cwgpu_get_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(Tuning)]),
+    "cwgpu_set_cta_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(CtaTuning)]),
+    "cwgpu_get_cta_tuning": (ctypes.c_int, [_vp, ctypes.POINTER(CtaTuning)]),
+    "cwgpu_cta_wait_probe": (ctypes.c_int, [_vp, _i64, ctypes.POINTER(ctypes.c_int32)]),
     "cwgpu_server_create": (
         ctypes.c_int,
         [ctypes.c_int, _vp, ctypes.POINTER(Params), ctypes.POINTER(ServerOpts), ctypes.POINTER(_vp)],
@@ -361,6 +371,25 @@ class Context:
         self._check(self._lib.cwgpu_get_tuning(self._h, ctypes.byref(t)), "cwgpu_get_tuning")
         return t.tiny_m, t.tiny_n, t.short_rows
 
+    def set_cta_tuning(self, max_pairs=None, warps=None, large_rows=None):
+        """Sets the knobs of cwgpu_cta_tuning; None keeps the current value."""
+        cur = self.get_cta_tuning()
+        t = CtaTuning(*(int(v if v is not None else c) for v, c in zip((max_pairs, warps, large_rows), cur)))
+        self._check(self._lib.cwgpu_set_cta_tuning(self._h, ctypes.byref(t)), "cwgpu_set_cta_tuning")
+
+    def get_cta_tuning(self):
+        t = CtaTuning()
+        self._check(self._lib.cwgpu_get_cta_tuning(self._h, ctypes.byref(t)), "cwgpu_get_cta_tuning")
+        return t.max_pairs, t.warps, t.large_rows
+
+    def cta_wait_probe(self, timeout_ns):
+        """True if the CTA form's hand-over wait, run on a word nothing raises,
+        ended at its limit with the timeout status."""
+        out = ctypes.c_int32(0)
+        self._check(self._lib.cwgpu_cta_wait_probe(self._h, int(timeout_ns), ctypes.byref(out)),
+                    "cwgpu_cta_wait_probe")
+        return bool(out.value)
+
     def synchronize(self):
         self._check(self._lib.cwgpu_synchronize(self._h), "cwgpu_synchronize")
 
@@ -395,6 +424,10 @@ class Plan:
     def kernel_count(self):
         """Kernels one launch of this plan runs (long-pair and/or short-pair)."""
         return int(self._lib.cwgpu_plan_kernel_count(self._h))
+
+    def pair_ctas(self):
+        """True if the plan's long pairs run one CTA per pair."""
+        return bool(self._lib.cwgpu_plan_pair_ctas(self._h))
 
     def device_dist_ptr(self):
         return self._lib.cwgpu_plan_device_dist(self._h)

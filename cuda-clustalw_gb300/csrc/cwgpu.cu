@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -83,6 +84,365 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
     }
 }
 
+// ---- one CTA per pair: the pair's stripes shared by the warps of a CTA ------
+//
+// For launches with fewer long pairs than the long-pair kernel has warps, one
+// warp per pair leaves most of the GPU idle. Here a CTA of nw warps aligns one
+// pair: forwardPass and reversePass are shared sweeps (cwgpu::sweep_mw) over
+// all nw warps, whose results are reduced across the warps; Myers-Miller
+// frames of at least large_rows rows are divided by the two halves of the CTA
+// at once (forward half on warps [0, nw/2), reverse half on [nw/2, nw)), and
+// the smaller frames they leave are shared out, one whole frame subtree per
+// warp (cwgpu::mm_align). Frames are independent once (A, B, M, N, tb, te) are
+// known and diff()'s identity and match counts are sums over its M == 1
+// leaves, so results equal those of the one-warp form.
+constexpr int kCtaMaxWarps = 16;
+constexpr int kCtaStack = 64;
+constexpr int kCtaSmall = 256;
+constexpr int kRootBit = 1 << 30;  // in Frame.z (M < 2^17): the pair's top frame
+
+struct CtaCtl {
+    unsigned long long prog[kCtaMaxWarps];  // cwgpu::MwSync progress words
+    int abort;
+    int stop;  // reversePass: lowest stripe that reached maxScore
+    long long q;
+    int bval[kCtaMaxWarps];
+    unsigned bkey[kCtaMaxWarps];
+    long long dcells[kCtaMaxWarps];
+    int ident[kCtaMaxWarps], match[kCtaMaxWarps];
+    int mm;  // diff()'s score of the pair
+    int nstack, nsmall, small_next;
+    int4 stack[kCtaStack];  // large frames: (A, B, M | root, N | tb << 29 | te << 30)
+    int4 small[kCtaSmall];  // frames for one warp each
+};
+
+struct CtaArgs {
+    int large_rows;
+    unsigned long long limit_ns;
+};
+
+// Maximum value, then lowest key, over the warps' results in C.
+__device__ __forceinline__ cwgpu::Best cta_reduce(const CtaCtl& C, int nw) {
+    cwgpu::Best b;
+    b.val = C.bval[0];
+    b.key = C.bkey[0];
+    for (int w = 1; w < nw; ++w) {
+        if (C.bval[w] > b.val || (C.bval[w] == b.val && C.bkey[w] < b.key)) {
+            b.val = C.bval[w];
+            b.key = C.bkey[w];
+        }
+    }
+    return b;
+}
+
+__device__ __forceinline__ bool cta_large(int M, int N, int large_rows) { return M >= large_rows && N >= 64; }
+
+// The small frames of C.small, one per warp at a time (every thread calls).
+template <int RS>
+__device__ void cta_small_frames(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, const int8_t* s2,
+                                 const int8_t* s2r, int m, int go, int ge, int2* bufA, int2* bufB, const cwgpu::Env& X,
+                                 int& ident, int& match, long long& cells) {
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x == 0) C.small_next = 0;
+    __syncthreads();
+    const int nsmall = C.nsmall;
+    for (;;) {
+        int k = 0;
+        if (lane == 0) k = atomicAdd(&C.small_next, 1);
+        k = __shfl_sync(cwgpu::kFull, k, 0);
+        if (k >= nsmall) break;
+        const int4 F = C.small[k];
+        int mmf = 0, id = 0, mt = 0;
+        long long ce = 0;
+        cwgpu::mm_align<RS>(s1, s1r, n, s2, s2r, m, F.x, F.y, F.z & ~kRootBit, F.w, go, ge, bufA, bufB, X, mmf, id, mt,
+                            ce);
+        ident += id;
+        match += mt;
+        cells += ce;
+        if ((F.z & kRootBit) && lane == 0) C.mm = mmf;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) C.nsmall = 0;
+    __syncthreads();
+}
+
+// diff() + tracePath of one pair by the whole CTA (every thread calls).
+template <int RS>
+__device__ void cta_diff(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, const int8_t* s2, const int8_t* s2r,
+                         int m, int A0, int B0, int M0, int N0, int go, int ge, int2* bufs, size_t stride, int nw,
+                         const cwgpu::Env& X, cwgpu::MwSync& mw, unsigned long long& epoch, const CtaArgs& ca,
+                         int& mm_score, int& n_ident, int& n_match, long long& cells) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int half = nw / 2;
+    int2* bufA = bufs + (size_t)warp * stride;
+    int2* bufB = bufA + stride / 2;
+    int ident = 0, match = 0;
+    long long ncell = 0;
+    if (threadIdx.x == 0) {
+        C.nstack = 0;
+        C.nsmall = 0;
+        C.mm = 0;
+        const int4 root = make_int4(A0, B0, M0 | kRootBit, N0);
+        if (cta_large(M0, N0, ca.large_rows))
+            C.stack[C.nstack++] = root;
+        else
+            C.small[C.nsmall++] = root;
+    }
+    __syncthreads();
+    for (;;) {
+        const int ns = C.nstack;
+        if (ns == 0) break;
+        const int4 F = C.stack[ns - 1];
+        __syncthreads();  // every thread has the frame before it is popped
+        if (threadIdx.x == 0) C.nstack = ns - 1;
+        const int A = F.x, B = F.y, M = F.z & ~kRootBit;
+        const int N = F.w & ((1 << 29) - 1);
+        const int tbf = (F.w >> 29) & 1, tef = (F.w >> 30) & 1;
+        const int tb = tbf ? go : 0, te = tef ? go : 0;
+        const int midi = M / 2;
+        const bool fwd_group = warp < half;
+        cwgpu::Task t;
+        if (fwd_group) {
+            t.rseq = s1 + A;
+            t.cseq = s2 + B;
+            t.rows = midi;
+            t.ht0 = t.hl0 = -tb;
+        } else {
+            t.rseq = s1r + (n - A - M);
+            t.cseq = s2r + (m - B - N);
+            t.rows = M - midi;
+            t.ht0 = t.hl0 = -te;
+        }
+        t.buf = nullptr;
+        t.cols = N;
+        t.hts = ge;
+        t.eo = go;
+        t.hls = ge;
+        t.fo = go;
+        mw.epoch = (++epoch) << 32;
+        cwgpu::Best unused;
+        cwgpu::sweep_mw<RS, cwgpu::MODE_GLOBAL>(t, go, ge, 0, X, unused, bufs, stride, fwd_group ? 0 : half,
+                                                fwd_group ? warp : warp - half, half, mw, &C.stop);
+        __syncthreads();
+        if (warp == 0) {
+            ncell += (long long)M * N;
+            const int2* fwd = bufs + (size_t)cwgpu::mw_last_rank(midi, RS, half) * stride;
+            const int2* rev = bufs + (size_t)(half + cwgpu::mw_last_rank(M - midi, RS, half)) * stride;
+            int midh, midj;
+            bool type2;
+            cwgpu::midpoint_scan(fwd, rev, M, N, midi, tb, te, go, ge, midh, midj, type2);
+            if (lane == 0) {
+                if (F.z & kRootBit) C.mm = midh;
+                int4 ch[2];  // right, then left, as diff() pushes them (:598-609)
+                if (!type2) {
+                    ch[0] = make_int4(A + midi, B + midj, M - midi, (N - midj) | (1 << 29) | (tef << 30));
+                    ch[1] = make_int4(A, B, midi, midj | (tbf << 29) | (1 << 30));
+                } else {
+                    ch[0] = make_int4(A + midi + 1, B + midj, M - midi - 1, (N - midj) | (tef << 30));
+                    ch[1] = make_int4(A, B, midi - 1, midj | (tbf << 29));
+                }
+                for (int c = 0; c < 2; ++c) {
+                    if (cta_large(ch[c].z, ch[c].w & ((1 << 29) - 1), ca.large_rows) && C.nstack < kCtaStack)
+                        C.stack[C.nstack++] = ch[c];
+                    else
+                        C.small[C.nsmall++] = ch[c];
+                }
+            }
+        }
+        __syncthreads();
+        if (C.nsmall > kCtaSmall - 2)
+            cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ident, match, ncell);
+    }
+    cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ident, match, ncell);
+    if (lane == 0) {
+        C.ident[warp] = ident;
+        C.match[warp] = match;
+        C.dcells[warp] = ncell;
+    }
+    __syncthreads();
+    n_ident = n_match = 0;
+    cells = 0;
+    for (int w = 0; w < nw; ++w) {
+        n_ident += C.ident[w];
+        n_match += C.match[w];
+        cells += C.dcells[w];
+    }
+    mm_score = C.mm;
+    __syncthreads();
+}
+
+// FullPairwiseAlign.cpp:112-183 for pair q by the whole CTA.
+template <int RS>
+__device__ void cta_pair(const cwgpu::PairArgs& g, long long q, CtaCtl& C, const cwgpu::Env& X, int2* bufs,
+                         size_t stride, int nw, const CtaArgs& ca, unsigned long long& epoch,
+                         unsigned long long (&acc)[3]) {
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int si = g.pairs[2 * q], sj = g.pairs[2 * q + 1];
+    const int n = g.lens[si], m = g.lens[sj];
+    const int8_t* s1 = g.codes + g.offs[si];
+    const int8_t* s2 = g.codes + g.offs[sj];
+    const int8_t* s1r = cwgpu::rev_of(s1, n);
+    const int8_t* s2r = cwgpu::rev_of(s2, m);
+    const int go = g.go_table[min(n, m)], ge = g.ge;
+    cwgpu_pair_stats st = cwgpu_pair_stats{0, 0, 0, 0, 0, 0, 0, 0};
+    float dist = 1.0f;
+    if (n > 0 && m > 0) {
+        cwgpu::MwSync mw;
+        mw.prog = C.prog;
+        mw.abort = &C.abort;
+        mw.err = g.err;
+        mw.limit_ns = ca.limit_ns;
+        // forwardPass
+        cwgpu::Task t;
+        t.rseq = s1;
+        t.cseq = s2;
+        t.rows = n;
+        t.cols = m;
+        t.ht0 = 0;
+        t.hts = 0;
+        t.eo = go;
+        t.hl0 = 0;
+        t.hls = 0;
+        t.fo = go;
+        t.buf = nullptr;
+        mw.epoch = (++epoch) << 32;
+        cwgpu::Best b;
+        cwgpu::sweep_mw<RS, cwgpu::MODE_LOCAL_FWD>(t, go, ge, 0, X, b, bufs, stride, 0, warp, nw, mw, &C.stop);
+        if (lane == 0) {
+            C.bval[warp] = b.val;
+            C.bkey[warp] = b.key;
+        }
+        __syncthreads();
+        const cwgpu::Best fb = cta_reduce(C, nw);
+        const int max_score = fb.val;
+        const int se1 = max_score > 0 ? (int)(fb.key >> 16) + 1 : 0;
+        const int se2 = max_score > 0 ? (int)(fb.key & 0xffffu) : 0;
+        __syncthreads();
+        if (threadIdx.x == 0) C.stop = INT_MAX;
+        __syncthreads();
+        // reversePass
+        int sb1 = 1, sb2 = 1;
+        if (se1 > 0) {
+            cwgpu::Task r;
+            r.rseq = s1r + (n - se1);
+            r.cseq = s2r + (m - se2);
+            r.rows = se1;
+            r.cols = se2;
+            r.ht0 = -1;
+            r.hts = 0;
+            r.eo = 0;
+            r.hl0 = -1;
+            r.hls = 0;
+            r.fo = 0;
+            r.buf = nullptr;
+            mw.epoch = (++epoch) << 32;
+            cwgpu::sweep_mw<RS, cwgpu::MODE_LOCAL_REV>(r, go, ge, max_score, X, b, bufs, stride, 0, warp, nw, mw,
+                                                       &C.stop);
+            if (lane == 0) {
+                C.bval[warp] = b.val;
+                C.bkey[warp] = b.key;
+            }
+            __syncthreads();
+            const cwgpu::Best rb = cta_reduce(C, nw);
+            __syncthreads();
+            if (rb.val > 0) {
+                sb1 = se1 - (int)(rb.key >> 16);
+                sb2 = se2 - (int)(rb.key & 0xffffu) + 1;
+            }
+            if (rb.val >= max_score)
+                acc[1] += (unsigned long long)(se1 - sb1) * se2 + (unsigned long long)(se2 - sb2 + 1);
+            else
+                acc[1] += (unsigned long long)se1 * se2;
+        }
+        acc[0] += (unsigned long long)n * m;
+        // diff + tracePath
+        int mm = 0, ident = 0, matches = 0;
+        long long dcells = 0;
+        cta_diff<RS>(C, s1, s1r, n, s2, s2r, m, sb1 - 1, sb2 - 1, se1 - sb1 + 1, se2 - sb2 + 1, go, ge, bufs, stride,
+                     nw, X, mw, epoch, ca, mm, ident, matches, dcells);
+        acc[2] += (unsigned long long)dcells;
+        // distance (:170-181), float arithmetic with IEEE rounding.
+        const int len1 = g.nres[si], len2 = g.nres[sj];
+        float mmv = (float)(100 * ident);
+        if (len1 == 0 || len2 == 0)
+            mmv = 0.0f;
+        else
+            mmv = __fdiv_rn(mmv, (float)min(len1, len2));
+        dist = __fdiv_rn(__fsub_rn(100.0f, mmv), 100.0f);
+        st.fwd_score = max_score;
+        st.se1 = se1;
+        st.se2 = se2;
+        st.sb1 = sb1;
+        st.sb2 = sb2;
+        st.mm_score = mm;
+        st.n_ident = ident;
+        st.n_match = matches;
+    }
+    if (threadIdx.x == 0) {
+        g.dist[q] = dist;
+        if (g.stats) g.stats[q] = st;
+    }
+}
+
+// Persistent: each CTA takes the next pair of the longest-first queue.
+__global__ void __launch_bounds__(kCtaMaxWarps * 32, 1) k_pairwise_cta(cwgpu::PairArgs g, CtaArgs ca) {
+    __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
+    __shared__ CtaCtl C;
+    extern __shared__ __align__(16) uint16_t region_all[];
+    for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = g.matrix[i];
+    const int nw = blockDim.x >> 5, warp = threadIdx.x >> 5;
+    if (threadIdx.x < kCtaMaxWarps) C.prog[threadIdx.x] = 0;
+    if (threadIdx.x == 0) {
+        C.abort = 0;
+        C.stop = INT_MAX;
+    }
+    cwgpu::Env X;
+    X.smat = smat;
+    X.region = region_all + (size_t)warp * (cwgpu::warp_region_bytes(g.K) / sizeof(uint16_t));
+    X.K = g.K;
+    X.gp1 = g.gp1;
+    X.gp2 = g.gp2;
+    X.tiny_m = g.tiny_m;
+    X.tiny_n = g.tiny_n;
+    X.err = g.err;
+    const size_t stride = 2 * (size_t)(g.lmax + 1);  // a warp's two rows
+    int2* bufs = g.scratch + (size_t)blockIdx.x * nw * stride;
+    __syncthreads();
+    unsigned long long epoch = 0;
+    unsigned long long acc[3] = {0, 0, 0};
+    for (;;) {
+        if (threadIdx.x == 0) C.q = (long long)atomicAdd(g.counter, 1ULL);
+        __syncthreads();
+        const long long k = C.q;
+        __syncthreads();
+        if (k >= g.npairs) break;
+        cta_pair<cwgpu::kR>(g, (long long)g.order[k], C, X, bufs, stride, nw, ca, epoch, acc);
+    }
+    if (threadIdx.x == 0 && g.cells && (acc[0] | acc[1] | acc[2])) {
+        atomicAdd(g.cells + 0, acc[0]);
+        atomicAdd(g.cells + 1, acc[1]);
+        atomicAdd(g.cells + 2, acc[2]);
+    }
+}
+
+// A wait of the shared sweeps on a progress word that nothing raises: warp 1
+// waits for warp 0, which publishes nothing. It must end at its limit with
+// the timeout status.
+__global__ void k_cta_wait_probe(int* err, unsigned long long limit_ns) {
+    __shared__ unsigned long long prog[2];
+    __shared__ int abort_flag;
+    if (threadIdx.x < 2) prog[threadIdx.x] = 0;
+    if (threadIdx.x == 0) abort_flag = 0;
+    __syncthreads();
+    cwgpu::MwSync mw;
+    mw.prog = prog;
+    mw.abort = &abort_flag;
+    mw.err = err;
+    mw.epoch = 1ULL << 32;
+    mw.limit_ns = limit_ns;
+    if ((threadIdx.x >> 5) == 1) cwgpu::mw_wait(mw, 0, cwgpu::mw_word(mw, 0, 1));
+}
+
 }  // namespace
 
 // struct cwgpu_context: cwgpu_context.h (shared with the quick-distance path).
@@ -95,6 +455,7 @@ struct cwgpu_plan {
     float* d_dist = nullptr;
     cwgpu_pair_stats* d_stats = nullptr;
     int64_t nlong = 0;  // order[0, nlong): long-pair kernel; order[nlong, npairs): short-pair kernel
+    bool ctas = false;  // the long pairs run one CTA per pair
     cudaGraph_t graph = nullptr;
     cudaGraphExec_t exec = nullptr;
     cudaStream_t graph_stream = nullptr;
@@ -206,10 +567,34 @@ bool has_short_seqs(const cwgpu_context* ctx) {
 // scratch holds one (bufA, bufB) pair per warp slot of the long-pair grid,
 // followed by the short-pair grid's slots when the set has short sequences
 // (the two kernels of a plan can run at the same time).
+size_t cta_smem(int K, int warps) { return block_smem(K, warps); }
+
+// CTAs of k_pairwise_cta that fit at once, capped so that their warps use no
+// more scratch slots than the long-pair kernel's grid (the short-pair kernel's
+// slots follow those, and it may run beside either).
+// 0 when the CTA's shared memory (a score-profile region per warp) does not
+// fit; launches then keep one warp per pair.
+int cta_grid(cwgpu_context* ctx, int warps, int* grid) {
+    int per_sm = 0, optin = 0;
+    const size_t smem = cta_smem(ctx->K, warps);
+    cudaFuncAttributes fa;
+    CW_CUDA(ctx, cudaFuncGetAttributes(&fa, k_pairwise_cta));
+    CW_CUDA(ctx, cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, ctx->device));
+    *grid = 0;
+    if (smem + fa.sharedSizeBytes > (size_t)optin) return CWGPU_OK;
+    CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise_cta, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      std::max(fa.maxDynamicSharedSizeBytes, (int)smem)));
+    CW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise_cta, warps * 32, smem));
+    if (per_sm < 1) return CWGPU_OK;
+    *grid = std::min(per_sm * ctx->sm_count, ctx->grid * kWarpsPerBlock / warps);
+    return CWGPU_OK;
+}
+
 int ensure_scratch(cwgpu_context* ctx) {
     if (ctx->grid == 0 || ctx->grid_K != ctx->K) {
         int rc = persistent_grid<cwgpu::kR>(ctx, &ctx->grid);
         if (!rc) rc = persistent_grid<cwgpu::kRShort>(ctx, &ctx->grid_short);
+        for (int l = 1; l <= 4 && !rc; ++l) rc = cta_grid(ctx, 1 << l, &ctx->grid_cta[l]);
         if (rc) return rc;
         ctx->grid_K = ctx->K;
         ctx->scratch_bytes = 0;  // grid changed: resize below
@@ -325,11 +710,55 @@ cudaError_t launch_persistent(const cwgpu::PairArgs& g, int max_grid, size_t sme
     return cudaLaunchKernelEx(&cfg, k_pairwise<RS>, g, -1LL);
 }
 
+// Warps per CTA for a launch of nlong long pairs: the knob, or, when it is 0,
+// 16 for at most half a pair per SM, 8 up to 2.5 pairs per SM, else 4
+// (measured on 3000- and 1523-residue families: 15 pairs 21.4 / 18.6 / 14.3
+// GCUPS with 16 / 8 / 4 warps; 190 pairs 137 / 171 / 151; 1,770 pairs 117 /
+// 187 / 248).
+int cta_warps_for(const cwgpu_context* ctx, int64_t nlong) {
+    if (ctx->cta_warps) return ctx->cta_warps;
+    if (2 * nlong <= ctx->sm_count) return 16;
+    if (2 * nlong <= 5 * (int64_t)ctx->sm_count) return 8;
+    return 4;
+}
+
+int log2_warps(int w) { return w >= 16 ? 4 : w >= 8 ? 3 : w >= 4 ? 2 : 1; }
+
+// One persistent launch of k_pairwise_cta over g's queue (one CTA per pair).
+cudaError_t launch_cta(const cwgpu_context* ctx, const cwgpu::PairArgs& g, int priority, cudaStream_t s) {
+    const int warps = cta_warps_for(ctx, g.npairs);
+    const int grid = (int)std::min<int64_t>(ctx->grid_cta[log2_warps(warps)], g.npairs);
+    CtaArgs ca;
+    ca.large_rows = ctx->cta_large_rows;
+    ca.limit_ns = 4000000000ULL;  // no legitimate hand-over waits this long
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(warps * 32);
+    cfg.dynamicSmemBytes = cta_smem(ctx->K, warps);
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributePriority;
+    attr[0].val.priority = priority;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_pairwise_cta, g, ca);
+}
+
+// Long pairs of a launch run one CTA per pair when there are few of them: at
+// most cta_pairs, or, by default, a quarter of the long-pair kernel's warps
+// (below that one warp per pair leaves most SMs idle; measured crossover on
+// 1523-residue families between 190 and 1,770 pairs).
+bool use_cta(const cwgpu_context* ctx, int64_t nlong) {
+    const int64_t limit = ctx->cta_pairs >= 0 ? ctx->cta_pairs : (int64_t)ctx->grid * kWarpsPerBlock / 4;
+    return nlong > 0 && nlong <= limit && ctx->grid_cta[log2_warps(cta_warps_for(ctx, nlong))] > 0;
+}
+
 // The queue-counter reset and one persistent launch per kernel: long pairs
 // on s, short pairs on s2 forked from s when both kinds are present (joined
 // back into s), else on s. The short-pair kernel runs at lower priority so
 // that its CTAs take the SM slots long-pair CTAs leave as the long queue
-// drains. Works the same under stream capture.
+// drains. Long pairs run one CTA per pair when there are at most cta_pairs of
+// them, else one warp per pair. Works the same under stream capture.
 cudaError_t enqueue_pairs(cwgpu_context* ctx, const cwgpu::PairArgs& gl, const cwgpu::PairArgs& gs, cudaStream_t s,
                           cudaStream_t s2, cudaEvent_t fork, cudaEvent_t join) {
     const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
@@ -341,7 +770,9 @@ cudaError_t enqueue_pairs(cwgpu_context* ctx, const cwgpu::PairArgs& gl, const c
         if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
         short_stream = s2;
     }
-    if (e == cudaSuccess && gl.npairs > 0) e = launch_persistent<cwgpu::kR>(gl, ctx->grid, smem, ctx->prio_high, s);
+    if (e == cudaSuccess && gl.npairs > 0)
+        e = use_cta(ctx, gl.npairs) ? launch_cta(ctx, gl, ctx->prio_high, s)
+                                    : launch_persistent<cwgpu::kR>(gl, ctx->grid, smem, ctx->prio_high, s);
     if (e == cudaSuccess && gs.npairs > 0)
         e = launch_persistent<cwgpu::kRShort>(gs, ctx->grid_short, smem, ctx->prio_low, short_stream);
     if (e == cudaSuccess && both) {
@@ -365,6 +796,8 @@ int check_kernel_error(cwgpu_context* ctx) {
     CW_CUDA(ctx, cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
     if (err) {
         CW_CUDA(ctx, cudaMemset(ctx->d_err, 0, sizeof(int)));
+        if (err == cwgpu::kStatusTimeout)
+            return fail(ctx, CWGPU_ERR_TIMEOUT, "a hand-over wait between the warps of a pair's CTA timed out");
         return fail(ctx, CWGPU_ERR_DEVICE, "kernel reported an internal limit (Myers-Miller stack depth)");
     }
     return CWGPU_OK;
@@ -616,6 +1049,7 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
         return cuda_fail(ctx, e, "cwgpu_plan_create");
     }
     p->generation = ctx->generation;
+    p->ctas = use_cta(ctx, p->nlong);
     *out = p;
     return CWGPU_OK;
 }
@@ -662,6 +1096,8 @@ int cwgpu_plan_kernel_count(const cwgpu_plan* p) {
     if (!p) return 0;
     return (p->nlong > 0 ? 1 : 0) + (p->npairs > p->nlong ? 1 : 0);
 }
+
+int cwgpu_plan_pair_ctas(const cwgpu_plan* p) { return p && p->ctas ? 1 : 0; }
 
 void cwgpu_plan_destroy(cwgpu_plan* p) {
     if (!p) return;
@@ -799,6 +1235,45 @@ int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning) {
     ctx->tiny_n = tuning->tiny_n;
     ctx->short_rows = tuning->short_rows;
     ctx->generation++;
+    return CWGPU_OK;
+}
+
+int cwgpu_set_cta_tuning(cwgpu_context* ctx, const cwgpu_cta_tuning* t) {
+    if (!ctx || !t) return CWGPU_ERR_ARG;
+    const int w = t->warps;
+    if (t->max_pairs < -1 || !(w == 0 || w == 2 || w == 4 || w == 8 || w == 16) || t->large_rows < 2 ||
+        t->large_rows > CWGPU_MAX_SEQ_LEN)
+        return fail(ctx, CWGPU_ERR_ARG,
+                    "max_pairs must be >= -1, warps 0, 2, 4, 8 or 16, large_rows in [2, 65535]");
+    ctx->cta_pairs = t->max_pairs;
+    ctx->cta_warps = w;
+    ctx->cta_large_rows = t->large_rows;
+    ctx->generation++;
+    return CWGPU_OK;
+}
+
+int cwgpu_get_cta_tuning(const cwgpu_context* ctx, cwgpu_cta_tuning* t) {
+    if (!ctx || !t) return CWGPU_ERR_ARG;
+    t->max_pairs = ctx->cta_pairs;
+    t->warps = ctx->cta_warps;
+    t->large_rows = ctx->cta_large_rows;
+    return CWGPU_OK;
+}
+
+int cwgpu_cta_wait_probe(cwgpu_context* ctx, int64_t timeout_ns, int32_t* timed_out) {
+    if (!ctx || !timed_out || timeout_ns < 1 || timeout_ns > 4000000000LL) return CWGPU_ERR_ARG;
+    *timed_out = 0;
+    CW_CUDA(ctx, cudaSetDevice(ctx->device));
+    CW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    int err = 0;
+    CW_CUDA(ctx, cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    if (err) return check_kernel_error(ctx);  // an earlier call's status first
+    k_cta_wait_probe<<<1, 64, 0, ctx->stream>>>(ctx->d_err, (unsigned long long)timeout_ns);
+    CW_CUDA(ctx, cudaGetLastError());
+    CW_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+    CW_CUDA(ctx, cudaMemcpy(&err, ctx->d_err, sizeof(int), cudaMemcpyDeviceToHost));
+    CW_CUDA(ctx, cudaMemset(ctx->d_err, 0, sizeof(int)));
+    *timed_out = err == cwgpu::kStatusTimeout ? 1 : 0;
     return CWGPU_OK;
 }
 

@@ -32,6 +32,12 @@ struct cwgpu_context {
     int code_of[CWGPU_NUMRES];       // dense index -> original code
     int tiny_m = 32, tiny_n = 16;    // Myers-Miller frames solved one per lane
     int short_rows = 128;            // pairs with a first sequence this short: short-pair kernel
+    // One CTA per pair (k_pairwise_cta) for launches of at most cta_pairs long
+    // pairs (-1: a quarter of the long-pair kernel's warps): cta_warps warps
+    // per CTA (0: chosen by pairs per SM), Myers-Miller frames of at least
+    // cta_large_rows rows divided by the whole CTA.
+    int cta_pairs = -1, cta_warps = 0, cta_large_rows = 512;
+    int grid_cta[5] = {0, 0, 0, 0, 0};  // CTAs of k_pairwise_cta that fit at once, by log2(warps), for grid_K
     int8_t* d_codes = nullptr;   // pair kernels' layout (cwgpu_layout.h): guards, forward and reversed copies
     int64_t* d_poffs = nullptr;  // forward copy of each sequence in d_codes
     int64_t* d_offs = nullptr;   // each sequence in host_codes (the quick path's upload of it)

@@ -165,6 +165,72 @@ __device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, c
     }
 }
 
+// ---------------------------------------------------- warps sharing one sweep
+
+// Device-side status values of the pair kernels' status word (nonzero = error).
+enum { kStatusStackLimit = 1, kStatusTimeout = 2 };
+
+// Hand-over of stripe boundary rows between the warps of a CTA that sweep one
+// task together (stripes dealt round-robin). Warp w writes the last row of
+// each of its stripes into its own row buffer and publishes how far it got in
+// its progress word: epoch | stripe << 17 | columns written, which only grows
+// (columns <= 65535, stripes <= 511, epochs count the CTA's sweeps). The warp
+// with the next stripe waits for that word before it loads a chunk of the
+// row. Every wait is bounded: past `limit_ns` it records kStatusTimeout, sets
+// `abort`, and every later wait of the CTA returns at once, so the kernel
+// ends (with wrong values that the host does not return).
+struct MwSync {
+    volatile unsigned long long* prog;  // shared: one progress word per warp of the CTA
+    volatile int* abort;                // shared
+    int* err;                           // global status word
+    unsigned long long epoch;           // the sweep's epoch, shifted left by 32
+    unsigned long long limit_ns;        // bound of one wait
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned long long mw_word(const MwSync& m, int stripe, int cols) {
+    return m.epoch | ((unsigned long long)stripe << 17) | (unsigned)cols;
+}
+
+// Warp-uniform: lane 0 waits until progress word `slot` reaches `target`.
+__device__ __forceinline__ void mw_wait(const MwSync& m, int slot, unsigned long long target) {
+    if ((threadIdx.x & 31) == 0 && m.prog[slot] < target && !*m.abort) {
+        const unsigned long long t0 = global_ns();
+        for (unsigned polls = 1;; ++polls) {
+            if (m.prog[slot] >= target || *m.abort) break;
+            if ((polls & 63) == 0 && global_ns() - t0 > m.limit_ns) {
+                *m.abort = 1;
+                atomicExch(m.err, kStatusTimeout);
+                break;
+            }
+        }
+    }
+    __threadfence_block();  // the row entries published before the word are read after it
+    __syncwarp();
+}
+
+// One lane: the row entries it wrote are visible to the CTA before the word.
+__device__ __forceinline__ void mw_publish(const MwSync& m, int slot, int stripe, int cols) {
+    __threadfence_block();
+    m.prog[slot] = mw_word(m, stripe, cols);
+}
+
+// Where a stripe's boundary rows come from and go to. Single-warp sweeps read
+// and write one buffer; in a shared sweep the row above comes from the
+// predecessor warp's buffer and the stripe's last row goes to the own one.
+struct StripeIO {
+    const int2* rbuf;
+    int2* wbuf;
+    int stripe;     // index of the stripe in the task
+    int pred_slot;  // progress word of the warp with the previous stripe
+    int own_slot;   // progress word of this warp
+};
+
 // The steps of one stripe. Lane sl processes column c = t - sl + 1 at step t.
 // Lane 0 of the segment takes the row above from the chunk registers (W columns
 // per lane-wide load: the previous stripe's last row, or the closed-form top
@@ -176,13 +242,18 @@ __device__ __forceinline__ void build_profile(uint16_t* prof, const int* smat, c
 // body. The next step's residue is loaded one step ahead from the lane's own
 // pointer, without clamping (the layout's guard bytes make the reads of fill
 // and drain steps safe; those residues are never used).
-template <int R, int W, int MODE, bool PARTIAL, bool NC>
+// MW: the stripe is one of a sweep shared by several warps (MwSync): before a
+// chunk of the row above is loaded the predecessor's progress is awaited, and
+// the writer publishes its progress every W columns and at the last one.
+template <int R, int W, int MODE, bool PARTIAL, bool NC, bool MW = false>
 __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T, SweepState<R>& S, int sl,
                                            int nvalid, bool writer, int ge, int goe, int thresh,
-                                           const uint16_t* prof_lane) {
+                                           const uint16_t* prof_lane, const StripeIO& io = StripeIO{},
+                                           const MwSync* mw = nullptr) {
     const unsigned ucols = (unsigned)T.cols;
-    const int8_t* cp = T.cseq - sl;  // residue of step t: cp[t]
-    int2* wp = T.buf + 1 - sl;       // boundary-row entry of step t: wp[t]
+    const int8_t* cp = T.cseq - sl;                 // residue of step t: cp[t]
+    int2* wp = (MW ? io.wbuf : T.buf) + 1 - sl;     // boundary-row entry of step t: wp[t]
+    const int2* rb = MW ? io.rbuf : T.buf;
     int bnext = ldres<NC>(cp);
     for (int t = 0; t < nsteps; ++t) {
         int hin = __shfl_up_sync(kFull, S.hout, 1, W);
@@ -201,10 +272,17 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
             if (first) {
                 S.nh = T.ht0 - col * T.hts;
                 S.ne = S.nh - T.eo + goe;
-            } else if (col <= T.cols) {
-                const int2 v = T.buf[col];
-                S.nh = v.x;
-                S.ne = v.y;
+            } else {
+                if constexpr (MW) {
+                    const int cfirst = (t / W + 2) * W + 1;
+                    if (cfirst <= T.cols)
+                        mw_wait(*mw, io.pred_slot, mw_word(*mw, io.stripe - 1, min(T.cols, cfirst + W - 1)));
+                }
+                if (col <= T.cols) {
+                    const int2 v = rb[col];
+                    S.nh = v.x;
+                    S.ne = v.y;
+                }
             }
         }
         const int b = bnext;
@@ -258,7 +336,13 @@ __device__ __forceinline__ void run_stripe(int nsteps, bool first, const Task& T
                     S.thr = sm;
                 }
             }
-            if (writer) wp[t] = make_int2(hup, eup);
+            if (writer) {
+                wp[t] = make_int2(hup, eup);
+                if constexpr (MW) {
+                    const int c = t - sl + 1;
+                    if ((c & (W - 1)) == 0 || c == T.cols) mw_publish(*mw, io.own_slot, io.stripe, c);
+                }
+            }
         }
     }
 }
@@ -362,6 +446,126 @@ __device__ void sweep(const Task& T, int go, int ge, int thresh, const Env& X, B
     }
     __syncwarp();
 }
+
+// A sweep shared by the nw warps of a group (ranks 0..nw-1, CTA warps
+// slot0 + rank): stripes of 32 x R rows are dealt round-robin, stripe s to rank
+// s % nw, and each stripe's last row goes to the buffer of its warp,
+// bufs + (slot0 + rank) * stride, from which the warp with the next stripe
+// reads it (MwSync). Every warp tracks the best of its own stripes the way
+// sweep() does (strict, so the first in row-major order); the caller reduces
+// the ranks' results: maximum value, then lowest key. MODE_LOCAL_REV: *stop
+// (shared, INT_MAX at the start) is lowered to every stripe that reached
+// thresh; stripes above it are skipped (their progress is published as
+// complete so no successor waits), which leaves the result of the lowest
+// such stripe, reversePass's break cell. MODE_GLOBAL: the final row is in the
+// buffer of rank (stripes - 1) % nw (see mw_last_rank).
+__host__ __device__ inline int mw_stripes(int rows, int R) { return rows > 0 ? (rows + 32 * R - 1) / (32 * R) : 0; }
+
+template <int R, int MODE, bool NC = true>
+__device__ void sweep_mw(const Task& T, int go, int ge, int thresh, const Env& X, Best& best, int2* bufs,
+                         size_t stride, int slot0, int rank, int nw, const MwSync& mw, volatile int* stop) {
+    constexpr int W = 32;
+    const int lane = threadIdx.x & 31;
+    const int sl = lane;
+    const int goe = go + ge;
+    constexpr int RPS = W * R;
+    const int nstr = mw_stripes(T.rows, R);
+    const uint16_t* prof_lane = X.region + lane * R;
+    best.val = 0;
+    best.key = 0xffffffffu;
+    if (T.cols <= 0) return;  // no column: nothing to hand over (callers give columns)
+    SweepState<R> S;
+    StripeIO io;
+    io.wbuf = bufs + (size_t)(slot0 + rank) * stride;
+    io.own_slot = slot0 + rank;
+
+    for (int s = rank; s < nstr; s += nw) {
+        io.stripe = s;
+        io.pred_slot = slot0 + (s + nw - 1) % nw;
+        io.rbuf = bufs + (size_t)io.pred_slot * stride;
+        if (MODE == MODE_LOCAL_REV && __shfl_sync(kFull, *stop, 0) < s) {  // one decision per warp
+            if (lane == 0) mw_publish(mw, io.own_slot, s, T.cols);
+            continue;
+        }
+        const int srow0 = s * RPS;
+        const int seg_rows = min(T.rows - srow0, RPS);
+        const int lrow0 = srow0 + sl * R;
+        const int nvalid = max(0, min(R, T.rows - lrow0));
+        const int lused = (seg_rows + R - 1) / R;
+        const int nsteps = T.cols > 0 ? T.cols + lused - 1 : 0;
+        const bool last = (s == nstr - 1);
+        const bool writer = (sl == lused - 1) && (MODE == MODE_GLOBAL || !last);
+        const bool full = seg_rows == RPS;
+
+        int a[R];
+#pragma unroll
+        for (int k = 0; k < R; ++k) a[k] = (k < nvalid) ? ldres<NC>(T.rseq + lrow0 + k) : 0;
+        __syncwarp();
+        build_profile<R>(X.region, X.smat, a, lane, X.K);
+        __syncwarp();
+
+        const int gbest = best.val;
+#pragma unroll
+        for (int k = 0; k < R; ++k) {
+            S.hl[k] = T.hl0 - (lrow0 + k + 1) * T.hls;
+            S.fp[k] = S.hl[k] - T.fo + goe;
+            S.rm[k] = gbest;
+            S.rc[k] = 0;
+        }
+        S.diag = (lrow0 == 0) ? 0 : T.hl0 - lrow0 * T.hls;
+        S.hout = 0;
+        S.eout = 0;
+        S.thr = gbest + 1;
+        const bool first = (s == 0);
+        if (first) {
+            S.ch = T.ht0 - (1 + sl) * T.hts;
+            S.ce = S.ch - T.eo + goe;
+            S.nh = T.ht0 - (W + 1 + sl) * T.hts;
+            S.ne = S.nh - T.eo + goe;
+        } else {
+            mw_wait(mw, io.pred_slot, mw_word(mw, s - 1, min(T.cols, 2 * W)));
+            S.ch = S.ce = S.nh = S.ne = 0;
+            if (1 + sl <= T.cols) {
+                const int2 v = io.rbuf[1 + sl];
+                S.ch = v.x;
+                S.ce = v.y;
+            }
+            if (W + 1 + sl <= T.cols) {
+                const int2 v = io.rbuf[W + 1 + sl];
+                S.nh = v.x;
+                S.ne = v.y;
+            }
+        }
+        if (full)
+            run_stripe<R, W, MODE, false, NC, true>(nsteps, first, T, S, sl, nvalid, writer, ge, goe, thresh,
+                                                    prof_lane, io, &mw);
+        else
+            run_stripe<R, W, MODE, true, NC, true>(nsteps, first, T, S, sl, nvalid, writer, ge, goe, thresh,
+                                                   prof_lane, io, &mw);
+
+        if (MODE != MODE_GLOBAL) {
+            int lv = gbest;
+            unsigned lk = 0xffffffffu;
+#pragma unroll
+            for (int k = 0; k < R; ++k) {
+                if (k < nvalid && S.rm[k] > lv) {
+                    lv = S.rm[k];
+                    lk = ((unsigned)(lrow0 + k) << 16) | (unsigned)S.rc[k];
+                }
+            }
+            const int wv = __reduce_max_sync(kFull, lv);
+            const unsigned wk = __reduce_min_sync(kFull, lv == wv ? lk : 0xffffffffu);
+            if (wv > best.val) {
+                best.val = wv;
+                best.key = wk;
+            }
+            if (MODE == MODE_LOCAL_REV && wv >= thresh && lane == 0) atomicMin((int*)stop, s);
+        }
+    }
+    __syncwarp();
+}
+
+__host__ __device__ inline int mw_last_rank(int rows, int R, int nw) { return (mw_stripes(rows, R) - 1) % nw; }
 
 // ---------------------------------------------------------------- tiny frames
 
@@ -508,6 +712,66 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
 
 // ---------------------------------------------------------------- diff()
 
+// Midpoint scans of a Myers-Miller frame (FullPairwiseAlign.cpp:570-593), by
+// one warp. fwd[j] holds (HH, DD + goe) of row midi from the forward half,
+// rev[N - j] holds (RR, SS + goe) of the same row from the reverse half (j =
+// 1..N and 0..N-1; the other ends are closed-form). Scan 1 keeps the first j
+// reaching the maximum of HH+RR, replaced by the last tied j with HH!=DD &&
+// RR==SS; scan 2 switches to a type-2 midpoint at the largest j whose
+// DD+SS+gapOpen is strictly above that maximum.
+__device__ __forceinline__ void midpoint_scan(const int2* fwd, const int2* rev, int M, int N, int midi, int tb, int te,
+                                              int go, int ge, int& midh, int& midj, bool& type2) {
+    const int lane = threadIdx.x & 31;
+    const int goe = go + ge;
+    const int HH0 = -tb - midi * ge;        // HH[0] = DD[0]
+    const int RRN = -te - (M - midi) * ge;  // RR[N] = SS[N]
+    int b1 = INT_MIN, j1 = 0x7fffffff, jc = -1, b2 = INT_MIN, j2 = -1;
+    for (int j = lane; j <= N; j += 32) {
+        int hh, dd, rr, ss;
+        if (j == 0) {
+            hh = dd = HH0;
+        } else {
+            const int2 v = fwd[j];
+            hh = v.x;
+            dd = v.y - goe;
+        }
+        if (j == N) {
+            rr = ss = RRN;
+        } else {
+            const int2 v = rev[N - j];
+            rr = v.x;
+            ss = v.y - goe;
+        }
+        const int v1 = hh + rr;
+        const bool cond = (hh != dd) && (rr == ss);
+        if (v1 > b1) {
+            b1 = v1;
+            j1 = j;
+            jc = cond ? j : -1;
+        } else if (v1 == b1 && cond) {
+            jc = j;
+        }
+        const int v2 = dd + ss + go;
+        if (v2 >= b2) {
+            b2 = v2;
+            j2 = j;
+        }
+    }
+    const int V = __reduce_max_sync(kFull, b1);
+    const int J1 = (int)__reduce_min_sync(kFull, b1 == V ? (unsigned)j1 : 0x7fffffffu);
+    const int JC = __reduce_max_sync(kFull, b1 == V ? jc : -1);
+    const int W2 = __reduce_max_sync(kFull, b2);
+    const int J2 = __reduce_max_sync(kFull, b2 == W2 ? j2 : -1);
+    midh = V;
+    midj = max(J1, JC);
+    type2 = false;
+    if (W2 > midh) {
+        midh = W2;
+        midj = J2;
+        type2 = true;
+    }
+}
+
 // Myers-Miller recursion (FullPairwiseAlign.cpp:418-612) for one pair. Large
 // frames are divided by the warp: forward half on lanes 0-15 and reverse half
 // on lanes 16-31, then the midpoint scans as warp reductions. Frames go on an
@@ -519,20 +783,21 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
 // gapOpen, kept as flags. s1/s2 are 0-based: the reference's 1-based residue
 // seq1[A + i] is s1[A + i - 1]. s1r/s2r are the reversed copies of the n- and
 // m-residue sequences (s1r[i] = s1[n - 1 - i]), which the reverse halves read.
+// N0 carries the top frame's flags: tb = gapOpen if bit 29, te if bit 30 (a
+// whole pair's frame has neither).
 template <int RS, bool NC = true>
 static __device__ void mm_align(const int8_t* s1, const int8_t* s1r, int n, const int8_t* s2, const int8_t* s2r, int m,
                                 int A0, int B0, int M0, int N0, int go, int ge, int2* bufA, int2* bufB, const Env& X,
                                 int& mm_score, int& n_ident, int& n_match, long long& cells) {
     const int lane = threadIdx.x & 31;
     constexpr int NMASK = (1 << 29) - 1;
-    const int goe = go + ge;
     int stA = 0, stB = 0, stM = 0, stN = 0;  // stack entry `lane`
     int qA = 0, qB = 0, qM = 0, qN = 0;      // tiny-queue entry `lane`
     if (lane == 0) {
         stA = A0;
         stB = B0;
         stM = M0;
-        stN = N0 & NMASK;
+        stN = N0;
     }
     int sp = 1, nq = 0;
     bool top = true;
@@ -649,56 +914,9 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s1r, int n, cons
         Best unused;
         sweep<RS, 16, MODE_GLOBAL, NC>(t, go, ge, 0, X, unused);
 
-        // Midpoint scans (:570-593). Scan 1 keeps the first j reaching the
-        // maximum of HH+RR, replaced by the last tied j with HH!=DD && RR==SS;
-        // scan 2 switches to a type-2 midpoint at the largest j whose
-        // DD+SS+gapOpen is strictly above that maximum. buf holds E' = E+goe.
-        const int HH0 = -tb - midi * ge;        // HH[0] = DD[0]
-        const int RRN = -te - (M - midi) * ge;  // RR[N] = SS[N]
-        int b1 = INT_MIN, j1 = 0x7fffffff, jc = -1, b2 = INT_MIN, j2 = -1;
-        for (int j = lane; j <= N; j += 32) {
-            int hh, dd, rr, ss;
-            if (j == 0) {
-                hh = dd = HH0;
-            } else {
-                const int2 v = bufA[j];
-                hh = v.x;
-                dd = v.y - goe;
-            }
-            if (j == N) {
-                rr = ss = RRN;
-            } else {
-                const int2 v = bufB[N - j];
-                rr = v.x;
-                ss = v.y - goe;
-            }
-            const int v1 = hh + rr;
-            const bool cond = (hh != dd) && (rr == ss);
-            if (v1 > b1) {
-                b1 = v1;
-                j1 = j;
-                jc = cond ? j : -1;
-            } else if (v1 == b1 && cond) {
-                jc = j;
-            }
-            const int v2 = dd + ss + go;
-            if (v2 >= b2) {
-                b2 = v2;
-                j2 = j;
-            }
-        }
-        const int V = __reduce_max_sync(kFull, b1);
-        const int J1 = (int)__reduce_min_sync(kFull, b1 == V ? (unsigned)j1 : 0x7fffffffu);
-        const int JC = __reduce_max_sync(kFull, b1 == V ? jc : -1);
-        const int W2 = __reduce_max_sync(kFull, b2);
-        const int J2 = __reduce_max_sync(kFull, b2 == W2 ? j2 : -1);
-        int midh = V, midj = max(J1, JC);
-        bool type2 = false;
-        if (W2 > midh) {
-            midh = W2;
-            midj = J2;
-            type2 = true;
-        }
+        int midh, midj;
+        bool type2;
+        midpoint_scan(bufA, bufB, M, N, midi, tb, te, go, ge, midh, midj, type2);
         if (top) mm = midh;
         top = false;
         __syncwarp();  // scan reads of bufA/bufB finish before the next sweep writes

@@ -172,6 +172,9 @@ void* cwgpu_plan_device_dist(cwgpu_plan* plan);
 int cwgpu_plan_cell_counts(cwgpu_plan* plan, int64_t* counts);
 /* Kernels one cwgpu_plan_launch runs (0, 1 or 2: long-pair and short-pair). */
 int cwgpu_plan_kernel_count(const cwgpu_plan* plan);
+/* 1 if the plan's long pairs run one CTA per pair (cwgpu_cta_tuning), 0 if
+ * one warp per pair. */
+int cwgpu_plan_pair_ctas(const cwgpu_plan* plan);
 void cwgpu_plan_destroy(cwgpu_plan* plan);
 
 /* ---- allocation-free variant ---------------------------------------------
@@ -215,6 +218,31 @@ typedef struct cwgpu_tuning {
 } cwgpu_tuning;
 int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning);
 int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning);
+
+/* One CTA per pair (no reference counterpart; results do not depend on it).
+ * A launch with at most max_pairs long pairs (first sequence longer than
+ * short_rows) runs them one CTA of `warps` warps (2, 4, 8 or 16) per pair
+ * instead of one warp per pair: the warps share the pair's forwardPass and
+ * reversePass stripes and every Myers-Miller frame of at least large_rows
+ * rows, and take the smaller frames one each. Defaults: max_pairs -1 (a
+ * quarter of the long-pair kernel's resident warps, 760 on a GB300), warps 0
+ * (16, 8 or 4 as the launch has at most 0.5, 2.5 or more pairs per SM),
+ * large_rows 512; max_pairs 0 turns it off. The reference's own GPU form also
+ * runs one CTA per pair (G/cuda/cudaFullPairwiseAlign.cu:369-468), as one
+ * 32-thread wavefront. A hand-over wait between the warps that ran out its
+ * bound ends the call with CWGPU_ERR_TIMEOUT. */
+typedef struct cwgpu_cta_tuning {
+    int32_t max_pairs;
+    int32_t warps;
+    int32_t large_rows;
+} cwgpu_cta_tuning;
+int cwgpu_set_cta_tuning(cwgpu_context* ctx, const cwgpu_cta_tuning* tuning);
+int cwgpu_get_cta_tuning(const cwgpu_context* ctx, cwgpu_cta_tuning* tuning);
+/* Diagnostic: runs the CTA form's hand-over wait on a progress word that
+ * nothing raises, limited to timeout_ns (1 .. 4e9). *timed_out is 1 when the
+ * wait ended at its limit with the timeout status, as every such wait must;
+ * the context stays usable. No GPU fault or hang is involved. */
+int cwgpu_cta_wait_probe(cwgpu_context* ctx, int64_t timeout_ns, int32_t* timed_out);
 
 /* ---- serving: continuous batching of independent jobs -----------------------
  * No counterpart in the reference (which aligns one sequence set per call).

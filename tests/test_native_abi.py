@@ -188,6 +188,52 @@ def test_autotune_search_and_cache_cpu(tmp_path, monkeypatch):
     assert choice2 == choice and timings2 == {} and ctx2.timed == [] and ctx2.get_tuning() == choice
 
 
+def test_autotune_cta_choice_cpu(monkeypatch):
+    """tune_cta on a stand-in context: the whole launch is timed one warp per
+    pair and with each CTA width, and the threshold is set so that a launch of
+    this many long pairs takes the faster form; launches with many long pairs
+    are not timed."""
+    from clustalw_gb300 import autotune, synth
+
+    class FakeCtx:
+        def __init__(self):
+            self.cta = (-1, 0, 512)
+            self.timed = []
+
+        def get_tuning(self):
+            return (32, 16, 128)
+
+        def get_cta_tuning(self):
+            return self.cta
+
+        def set_cta_tuning(self, p, w, r):
+            self.cta = (p, w, r)
+
+    def fake_time(cost):
+        def f(ctx, sample, repeats):
+            ctx.timed.append(ctx.cta)
+            return cost(ctx.cta)
+        return f
+
+    lens = np.array([1500] * 10 + [100] * 5)
+    pairs = synth.all_pairs(len(lens))  # 95 long pairs (first sequence > 128), 10 short
+    # CTA form with 8 warps fastest
+    monkeypatch.setattr(autotune, "_time_sample", fake_time(lambda t: 1.0 if t[0] == 0 else abs(t[1] - 8) + 0.5))
+    ctx = FakeCtx()
+    choice, timings = autotune.tune_cta(ctx, lens, pairs)
+    assert choice == (95, 8, 512) and ctx.cta == choice and len(timings) == 1 + len(autotune.CTA_WARPS)
+    # one warp per pair fastest: the threshold falls below this launch
+    monkeypatch.setattr(autotune, "_time_sample", fake_time(lambda t: 0.5 if t[0] == 0 else 1.0))
+    ctx = FakeCtx()
+    choice, _ = autotune.tune_cta(ctx, lens, pairs)
+    assert choice[0] == 94 and ctx.cta == choice
+    # many long pairs: untimed
+    ctx = FakeCtx()
+    big = np.array([1500] * 100)
+    choice, timings = autotune.tune_cta(ctx, big, synth.all_pairs(100))
+    assert timings == {} and ctx.timed == [] and choice == (-1, 0, 512)
+
+
 def test_missing_library_fails_loudly(monkeypatch, tmp_path):
     """No CPU fallback: without the built library the package raises instead
     of computing anything."""
