@@ -501,41 +501,94 @@ cudaError_t grow(T*& p, int64_t& cap, int64_t need) {
     return e;
 }
 
-// Recomputes nres and the gap-open table after sequences or params changed.
-int refresh_derived(cwgpu_context* ctx) {
-    if (!ctx->derived_dirty) return CWGPU_OK;
-    if (!ctx->has_params || !ctx->has_seqs) return fail(ctx, CWGPU_ERR_STATE, "params or sequences not set");
+cudaError_t pinned_grow(unsigned char*& p, size_t& cap, size_t need) {
+    if (need <= cap && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMallocHost(&p, std::max<size_t>(need, 4096));
+    if (e == cudaSuccess) cap = std::max<size_t>(need, 4096);
+    return e;
+}
+
+// Everything the pair kernels and the quick path read, in one arena: the code
+// layout, both offset arrays and the lengths; with params, the residue counts
+// (len1/len2 of FullPairwiseAlign.cpp:100-127) and the gap-open table by
+// min(n, m) (:129-146); with the matrix, the matrix over the dense codes.
+// One copy from one pinned buffer, on the context's stream, so later work on
+// that stream sees it; the staging buffer is reused only after that copy.
+int stage_inputs(cwgpu_context* ctx) {
+    if (!ctx->in_dirty) return CWGPU_OK;
+    if (!ctx->has_seqs) return fail(ctx, CWGPU_ERR_STATE, "sequences not uploaded");
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
-    std::vector<int32_t> nres(ctx->nseqs);
-    for (int s = 0; s < ctx->nseqs; ++s) {
-        int c = 0;
-        const int8_t* p = ctx->host_codes.data() + ctx->offs[s];
-        for (int i = 0; i < ctx->lens[s]; ++i)
-            if (p[i] != ctx->params.gap_pos1 && p[i] != ctx->params.gap_pos2) ++c;
-        nres[s] = c;
+    const int ns = ctx->nseqs;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t o_codes = 0;
+    const size_t o_poffs = o_codes + up(ctx->host_layout.size());
+    const size_t o_offs = o_poffs + up(8 * (size_t)ns);
+    const size_t o_lens = o_offs + up(8 * (size_t)ns);
+    const size_t o_nres = o_lens + up(4 * (size_t)ns);
+    const size_t o_go = o_nres + up(4 * (size_t)ns);
+    const size_t o_mat = o_go + up(4 * (size_t)(ctx->lmax + 1));
+    const size_t total = o_mat + 4 * CWGPU_NUMRES * CWGPU_NUMRES;
+    if (total > ctx->cap_in) {
+        dfree(ctx->d_in);
+        ctx->cap_in = 0;
+        CW_CUDA(ctx, cudaMalloc(&ctx->d_in, total));
+        ctx->cap_in = total;
     }
-    if (ctx->nseqs)
-        CW_CUDA(ctx, cudaMemcpy(ctx->d_nres, nres.data(), sizeof(int32_t) * ctx->nseqs, cudaMemcpyHostToDevice));
-    std::vector<int32_t> go(ctx->lmax + 1);
-    for (int L = 1; L <= ctx->lmax; ++L) {  // L = 0 pairs never reach the penalties (:113-118)
-        int32_t g = 0, e = 0;
-        cwgpu_gap_penalties(&ctx->params, L, L, &g, &e);
-        go[L] = g;
+    if (!ctx->ev_in) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming));
+    CW_CUDA(ctx, cudaEventSynchronize(ctx->ev_in));  // the previous staging copy is done
+    CW_CUDA(ctx, pinned_grow(ctx->h_in, ctx->cap_h_in, total));
+    unsigned char* h = ctx->h_in;
+    memcpy(h + o_codes, ctx->host_layout.data(), ctx->host_layout.size());
+    memcpy(h + o_poffs, ctx->host_poffs.data(), 8 * (size_t)ns);
+    memcpy(h + o_offs, ctx->offs.data(), 8 * (size_t)ns);
+    memcpy(h + o_lens, ctx->lens.data(), 4 * (size_t)ns);
+    if (ctx->has_params) {
+        int32_t* nres = reinterpret_cast<int32_t*>(h + o_nres);
+        for (int s = 0; s < ns; ++s) {
+            int c = 0;
+            const int8_t* p = ctx->host_codes.data() + ctx->offs[s];
+            for (int i = 0; i < ctx->lens[s]; ++i)
+                if (p[i] != ctx->params.gap_pos1 && p[i] != ctx->params.gap_pos2) ++c;
+            nres[s] = c;
+        }
+        int32_t* go = reinterpret_cast<int32_t*>(h + o_go);
+        go[0] = 0;  // L = 0 pairs never reach the penalties (:113-118)
+        for (int L = 1; L <= ctx->lmax; ++L) {
+            int32_t g = 0, e = 0;
+            cwgpu_gap_penalties(&ctx->params, L, L, &g, &e);
+            go[L] = g;
+        }
     }
-    CW_CUDA(ctx, grow(ctx->d_go, ctx->cap_go, (int64_t)go.size()));
-    CW_CUDA(ctx, cudaMemcpy(ctx->d_go, go.data(), sizeof(int32_t) * go.size(), cudaMemcpyHostToDevice));
-    ctx->go_len = (int)go.size();
-    // Matrix over the dense codes, row stride 32 (entries past K unused).
-    if (ctx->has_matrix) {
-        std::vector<int32_t> dm(CWGPU_NUMRES * CWGPU_NUMRES, 0);
+    if (ctx->has_matrix) {  // over the dense codes, row stride 32 (entries past K unused)
+        int32_t* dm = reinterpret_cast<int32_t*>(h + o_mat);
+        memset(dm, 0, 4 * CWGPU_NUMRES * CWGPU_NUMRES);
         for (int a = 0; a < ctx->K; ++a)
             for (int b = 0; b < ctx->K; ++b)
                 dm[a * CWGPU_NUMRES + b] = ctx->matrix[ctx->code_of[a] * CWGPU_NUMRES + ctx->code_of[b]];
-        CW_CUDA(ctx, cudaMemcpy(ctx->d_matrix, dm.data(), sizeof(int32_t) * dm.size(), cudaMemcpyHostToDevice));
     }
-    ctx->derived_dirty = false;
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_in, h, total, cudaMemcpyHostToDevice, ctx->stream));
+    CW_CUDA(ctx, cudaEventRecord(ctx->ev_in, ctx->stream));
+    unsigned char* d = ctx->d_in;
+    ctx->d_codes = reinterpret_cast<int8_t*>(d + o_codes);
+    ctx->d_poffs = reinterpret_cast<int64_t*>(d + o_poffs);
+    ctx->d_offs = reinterpret_cast<int64_t*>(d + o_offs);
+    ctx->d_lens = reinterpret_cast<int32_t*>(d + o_lens);
+    ctx->d_nres = ctx->has_params ? reinterpret_cast<int32_t*>(d + o_nres) : nullptr;
+    ctx->d_go = ctx->has_params ? reinterpret_cast<int32_t*>(d + o_go) : nullptr;
+    ctx->go_len = ctx->lmax + 1;
+    ctx->d_matrix = ctx->has_matrix ? reinterpret_cast<int32_t*>(d + o_mat) : nullptr;
+    ctx->in_dirty = false;
     ctx->generation++;
     return CWGPU_OK;
+}
+
+// The pair path needs params, matrix and sequences on the device.
+int refresh_derived(cwgpu_context* ctx) {
+    if (!ctx->has_params || !ctx->has_seqs) return fail(ctx, CWGPU_ERR_STATE, "params or sequences not set");
+    return stage_inputs(ctx);
 }
 
 int gap_extend_of(const cwgpu_params& p) {
@@ -805,6 +858,8 @@ int check_kernel_error(cwgpu_context* ctx) {
 
 }  // namespace
 
+int cwgpu_stage_inputs(cwgpu_context* ctx) { return stage_inputs(ctx); }
+
 extern "C" {
 
 const char* cwgpu_status_string(int status) {
@@ -869,7 +924,6 @@ int cwgpu_create(int device, cwgpu_context** out) {
     if (e == cudaSuccess) e = cudaMemset(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long));
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_err, 0, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_matrix, sizeof(int32_t) * CWGPU_NUMRES * CWGPU_NUMRES);
     if (e != cudaSuccess) {
         cwgpu_destroy(ctx);
         return e == cudaErrorMemoryAllocation ? CWGPU_ERR_OOM : CWGPU_ERR_CUDA;
@@ -883,13 +937,10 @@ void cwgpu_destroy(cwgpu_context* ctx) {
     if (!ctx) return;
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
-    dfree(ctx->d_codes);
-    dfree(ctx->d_poffs);
-    dfree(ctx->d_offs);
-    dfree(ctx->d_lens);
-    dfree(ctx->d_nres);
-    dfree(ctx->d_matrix);
-    dfree(ctx->d_go);
+    dfree(ctx->d_in);
+    if (ctx->h_in) cudaFreeHost(ctx->h_in);
+    if (ctx->h_io) cudaFreeHost(ctx->h_io);
+    if (ctx->ev_in) cudaEventDestroy(ctx->ev_in);
     dfree(ctx->d_scratch);
     dfree(ctx->d_counter);
     dfree(ctx->d_err);
@@ -914,7 +965,7 @@ int cwgpu_set_matrix(cwgpu_context* ctx, const int32_t* matrix) {
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
     memcpy(ctx->matrix, matrix, sizeof(ctx->matrix));
     ctx->has_matrix = true;
-    ctx->derived_dirty = true;  // the device copy is remapped to the dense codes
+    ctx->in_dirty = true;  // the device copy is remapped to the dense codes
     ctx->generation++;
     return CWGPU_OK;
 }
@@ -923,7 +974,7 @@ int cwgpu_set_params(cwgpu_context* ctx, const cwgpu_params* params) {
     if (!ctx || !params) return CWGPU_ERR_ARG;
     ctx->params = *params;
     ctx->has_params = true;
-    ctx->derived_dirty = true;
+    ctx->in_dirty = true;
     ctx->generation++;
     return CWGPU_OK;
 }
@@ -968,28 +1019,10 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     std::vector<int64_t> poffs;
     cwgpu::build_layout(
         nseqs, lens, [&](int s, int i) { return (int8_t)dense_of[codes[offsets[s] + i]]; }, dense, poffs);
-    CW_CUDA(ctx, cudaSetDevice(ctx->device));
-    ctx->has_seqs = false;
-    CW_CUDA(ctx, grow(ctx->d_codes, ctx->cap_codes, (int64_t)dense.size()));
-    if (nseqs > ctx->cap_seqs || !ctx->d_offs || !ctx->d_poffs || !ctx->d_lens || !ctx->d_nres) {
-        int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
-        dfree(ctx->d_offs);
-        dfree(ctx->d_poffs);
-        dfree(ctx->d_lens);
-        dfree(ctx->d_nres);
-        ctx->cap_seqs = 0;
-        CW_CUDA(ctx, grow(ctx->d_offs, c1, nseqs));
-        CW_CUDA(ctx, grow(ctx->d_poffs, c4, nseqs));
-        CW_CUDA(ctx, grow(ctx->d_lens, c2, nseqs));
-        CW_CUDA(ctx, grow(ctx->d_nres, c3, nseqs));
-        ctx->cap_seqs = c1;
-    }
-    CW_CUDA(ctx, cudaMemcpy(ctx->d_codes, dense.data(), dense.size(), cudaMemcpyHostToDevice));
-    if (nseqs) {
-        CW_CUDA(ctx, cudaMemcpy(ctx->d_offs, doffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
-        CW_CUDA(ctx, cudaMemcpy(ctx->d_poffs, poffs.data(), sizeof(int64_t) * nseqs, cudaMemcpyHostToDevice));
-        CW_CUDA(ctx, cudaMemcpy(ctx->d_lens, lens, sizeof(int32_t) * nseqs, cudaMemcpyHostToDevice));
-    }
+    // The device copy is made by the next call that needs it (stage_inputs),
+    // in one copy together with the tables derived from params and matrix.
+    ctx->host_layout.swap(dense);
+    ctx->host_poffs.swap(poffs);
     ctx->nseqs = nseqs;
     ctx->lmax = lmax;
     ctx->lens.assign(lens, lens + nseqs);
@@ -999,7 +1032,7 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     memcpy(ctx->dense_of, dense_of, sizeof(dense_of));
     memcpy(ctx->code_of, code_of, sizeof(code_of));
     ctx->has_seqs = true;
-    ctx->derived_dirty = true;
+    ctx->in_dirty = true;
     ctx->generation++;
     return CWGPU_OK;
 }
@@ -1057,7 +1090,7 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
 int cwgpu_plan_launch(cwgpu_plan* p, void* stream) {
     if (!p) return CWGPU_ERR_ARG;
     cwgpu_context* ctx = p->ctx;
-    if (p->generation != ctx->generation || ctx->derived_dirty)
+    if (p->generation != ctx->generation || ctx->in_dirty)
         return fail(ctx, CWGPU_ERR_STATE, "plan is stale: inputs changed after cwgpu_plan_create");
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
     cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
@@ -1141,21 +1174,37 @@ int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
     if (!ctx->stream_short) CW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream_short, cudaStreamNonBlocking));
     if (!ctx->ev_fork) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
     if (!ctx->ev_join) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
+    // Pair list and work order in, distances, statistics and the status word
+    // out, all through one pinned buffer: asynchronous copies on the stream
+    // and a single synchronization at the end.
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    const size_t n = (size_t)npairs;
+    const size_t o_order = up(8 * n), o_dist = o_order + up(4 * n);
+    const size_t o_stats = o_dist + up(4 * n), o_err = o_stats + up(sizeof(cwgpu_pair_stats) * n);
+    CW_CUDA(ctx, pinned_grow(ctx->h_io, ctx->cap_h_io, o_err + 4));
     int64_t nlong = 0;
     const std::vector<int32_t> order = work_order(ctx, pairs, npairs, &nlong);
+    memcpy(ctx->h_io, pairs, 8 * n);
+    memcpy(ctx->h_io + o_order, order.data(), 4 * n);
     cudaStream_t s = ctx->stream;
-    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs1, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice, s));
-    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_order1, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice, s));
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs1, ctx->h_io, 8 * n, cudaMemcpyHostToDevice, s));
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_order1, ctx->h_io + o_order, 4 * n, cudaMemcpyHostToDevice, s));
     cwgpu::PairArgs gl, gs;
     split_args(ctx, ctx->d_pairs1, ctx->d_order1, npairs, nlong, ctx->d_dist1, stats_out ? ctx->d_stats1 : nullptr,
                &gl, &gs);
     CW_CUDA(ctx, enqueue_pairs(ctx, gl, gs, s, ctx->stream_short, ctx->ev_fork, ctx->ev_join));
-    CW_CUDA(ctx, cudaMemcpyAsync(dist_out, ctx->d_dist1, sizeof(float) * npairs, cudaMemcpyDeviceToHost, s));
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->h_io + o_dist, ctx->d_dist1, 4 * n, cudaMemcpyDeviceToHost, s));
     if (stats_out)
-        CW_CUDA(ctx, cudaMemcpyAsync(stats_out, ctx->d_stats1, sizeof(cwgpu_pair_stats) * npairs,
+        CW_CUDA(ctx, cudaMemcpyAsync(ctx->h_io + o_stats, ctx->d_stats1, sizeof(cwgpu_pair_stats) * n,
                                      cudaMemcpyDeviceToHost, s));
+    CW_CUDA(ctx, cudaMemcpyAsync(ctx->h_io + o_err, ctx->d_err, 4, cudaMemcpyDeviceToHost, s));
     CW_CUDA(ctx, cudaStreamSynchronize(s));
-    return check_kernel_error(ctx);
+    int err = 0;
+    memcpy(&err, ctx->h_io + o_err, 4);
+    if (err) return check_kernel_error(ctx);
+    memcpy(dist_out, ctx->h_io + o_dist, 4 * n);
+    if (stats_out) memcpy(stats_out, ctx->h_io + o_stats, sizeof(cwgpu_pair_stats) * n);
+    return CWGPU_OK;
 }
 
 int cwgpu_align_pairs_plain(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, float* dist_out,

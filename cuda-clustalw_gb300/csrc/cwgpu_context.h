@@ -14,6 +14,9 @@
 struct cwgpu_fast_state;
 // Frees the quick-distance tables of a context (cwgpu_fast.cu).
 void cwgpu_fast_release(cwgpu_context* ctx);
+// Copies inputs changed on the host since the last call into the context's
+// device arena (one asynchronous copy on ctx->stream); cwgpu.cu.
+int cwgpu_stage_inputs(cwgpu_context* ctx);
 
 struct cwgpu_context {
     int device = 0;
@@ -38,13 +41,24 @@ struct cwgpu_context {
     // cta_large_rows rows divided by the whole CTA.
     int cta_pairs = -1, cta_warps = 0, cta_large_rows = 512;
     int grid_cta[5] = {0, 0, 0, 0, 0};  // CTAs of k_pairwise_cta that fit at once, by log2(warps), for grid_K
+    // Inputs on the device: one arena, filled by one copy from one pinned
+    // staging buffer whenever the host-side inputs changed (cwgpu_stage_inputs).
+    // The pointers below point into it.
+    unsigned char* d_in = nullptr;
+    size_t cap_in = 0;
+    unsigned char* h_in = nullptr;  // pinned staging of the arena
+    size_t cap_h_in = 0;
+    cudaEvent_t ev_in = nullptr;    // recorded after the last staging copy
+    bool in_dirty = true;
+    std::vector<int8_t> host_layout;  // d_codes as built on the host
+    std::vector<int64_t> host_poffs;
     int8_t* d_codes = nullptr;   // pair kernels' layout (cwgpu_layout.h): guards, forward and reversed copies
     int64_t* d_poffs = nullptr;  // forward copy of each sequence in d_codes
     int64_t* d_offs = nullptr;   // each sequence in host_codes (the quick path's upload of it)
     int32_t* d_lens = nullptr;
-    int32_t* d_nres = nullptr;
-    int32_t* d_matrix = nullptr;
-    int32_t* d_go = nullptr;
+    int32_t* d_nres = nullptr;   // set once params are
+    int32_t* d_matrix = nullptr; // set once the matrix is
+    int32_t* d_go = nullptr;     // set once params are
     int go_len = 0;
     int2* d_scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -53,12 +67,13 @@ struct cwgpu_context {
     int grid = 0;        // persistent CTAs of the long-pair kernel
     int grid_short = 0;  // and of the short-pair kernel
     int grid_K = -1;  // K the grid size was computed for
-    bool derived_dirty = true;
     unsigned generation = 0;  // bumped whenever device inputs or scratch move
     std::string last_error;
     cwgpu_fast_state* fast = nullptr;  // quick-distance tables (cwgpu_fast.cu), built on first use
-    // Grow-only device arrays of the inputs (capacities in elements).
-    int64_t cap_codes = 0, cap_seqs = 0, cap_go = 0;
+    // One-shot cwgpu_align_pairs: pinned staging of the pair list in and the
+    // distances, statistics and status word out.
+    unsigned char* h_io = nullptr;
+    size_t cap_h_io = 0;
     // One-shot cwgpu_align_pairs: grow-only pair arrays and the second stream
     // the short-pair kernel runs on beside the long-pair one.
     int32_t* d_pairs1 = nullptr;

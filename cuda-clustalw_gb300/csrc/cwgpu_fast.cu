@@ -713,6 +713,8 @@ int make_params(cwgpu_context* ctx, const cwgpu_fast_params* p, Params* P) {
 }
 
 int ensure_tables(cwgpu_context* ctx, const Params& P) {
+    const int rc = cwgpu_stage_inputs(ctx);  // offsets and lengths on the device
+    if (rc) return rc;
     if (!ctx->fast) ctx->fast = new cwgpu_fast_state();
     cwgpu_fast_state* F = ctx->fast;
     if (F->generation == ctx->generation && F->key_dna == P.dna && F->key_ktup == P.ktup &&
