@@ -77,6 +77,8 @@ def parse_args():
     ap.add_argument("--serve-seconds", type=float, default=12.0, help="length of the served arrival process")
     ap.add_argument("--serve-rate", type=float, default=6.0, help="served job arrival rate (jobs/s)")
     ap.add_argument("--no-serve", action="store_true")
+    ap.add_argument("--serve-only", action="store_true",
+                    help="only the served stream, for --serve-seconds (use 600 for the stated configuration)")
     ap.add_argument("--no-tree", action="store_true", help="skip the guide-tree leg")
     ap.add_argument("--no-quick", action="store_true", help="skip the quick k-tuple distance leg")
     ap.add_argument("--no-few", action="store_true",
@@ -432,6 +434,29 @@ def served_leg(args, matrix, params, device):
             srv.wait(jid)
             srv.release(jid)
         burst_s = time.perf_counter() - t
+    # The batched form on the same job mix: every job's sequences in one
+    # context, the pairs within each job in one plan, one launch.
+    offs, base, codes_all, lens_all, pairs_all = [], 0, [], [], []
+    pos = 0
+    for pk in jobs:
+        c, o, ln = pk
+        codes_all.append(c)
+        offs.append(o + pos)
+        lens_all.append(ln)
+        pairs_all.append(synth.all_pairs(len(ln)) + base)
+        pos += len(c)
+        base += len(ln)
+    mix = (np.concatenate(codes_all), np.concatenate(offs).astype(np.int64), np.concatenate(lens_all))
+    pairs_mix = np.concatenate(pairs_all).astype(np.int32)
+    with native.Context(device) as cm:
+        cm.set_matrix(matrix)
+        cm.set_params(params)
+        cm.upload_seqs(packed=mix)
+        plan = cm.plan(pairs_mix)
+        import torch
+
+        ms_mix = _time_plan(plan, torch.cuda.Stream(), 2)
+        plan.close()
     # The same arrivals in admission order.
     with Server(matrix, params, device=device, memory_budget=40 << 30, max_seq_len=2048, round_cells=6e9,
                 policy="fifo") as srv:
@@ -449,6 +474,8 @@ def served_leg(args, matrix, params, device):
         "capacity_gcups": sum(cells) / burst_s / 1e9,
         "plain_per_job_gcups": c_plain / t_plain / 1e9,
         "capacity_over_plain_per_job": (sum(cells) / burst_s) / (c_plain / t_plain),
+        "batched_same_mix_gcups": sum(cells) / (ms_mix / 1e3) / 1e9,
+        "capacity_over_batched_same_mix": (sum(cells) / burst_s) / (sum(cells) / (ms_mix / 1e3)),
         "plain_sample_jobs": len(sample),
         "rounds": info["rounds"],
         "policy": "least remaining work first; jobs older than 500 ms first, in admission order",
@@ -457,6 +484,78 @@ def served_leg(args, matrix, params, device):
         "budget_bytes": 40 << 30,
         "workload": "protein families, N ~ U[10,500], root length ~ U[50,1500], Poisson arrivals",
     }
+
+
+def _make_job(spec):
+    from clustalw_gb300 import native, synth
+
+    n, L, sd = spec
+    return native.pack_sequences(synth.protein_family(n, L, sd))
+
+
+def serve_only(args):
+    """The served configuration at its stated length: Poisson arrivals at
+    --serve-rate jobs/s for --serve-seconds (default here 600 s), jobs from the
+    served generator (protein families, N ~ U[10, 500], root length ~ U[50,
+    1500]), 40 GB budget, least remaining work first with a 500 ms age cap.
+    Jobs are generated before the run on all host cores (spawned workers, before
+    any device call). Prints one JSON line with the latency distribution over
+    every job, the arrival rate, the offered GCUPS and the memory peak."""
+    import multiprocessing as mp
+
+    from clustalw_gb300 import load_matrix, synth
+
+    njobs = max(4, int(round(args.serve_rate * args.serve_seconds)))
+    spec = synth.serve_jobs(njobs, seed=args.seed)
+    t = time.perf_counter()
+    with mp.get_context("spawn").Pool(os.cpu_count() or 1) as pool:
+        jobs = pool.map(_make_job, spec, chunksize=8)
+    gen_s = time.perf_counter() - t
+    cells = [int((int(ln.sum()) ** 2 - int((ln.astype(np.int64) ** 2).sum())) // 2) for _, _, ln in jobs]
+
+    import torch
+
+    from clustalw_gb300.serve import Server, percentile, run_arrivals
+
+    _, _, local = dist_env()
+    torch.cuda.set_device(local)
+    matrix, params = load_matrix("protein")
+    peaks = {}
+    with Server(matrix, params, device=local, memory_budget=40 << 30, max_seq_len=2048, round_cells=6e9,
+                policy="srpt", srpt_age_ms=500) as srv:
+        for k in range(2):  # warm-up jobs
+            srv.wait(srv.submit(packed=jobs[k]))
+        uuid = getattr(torch.cuda.get_device_properties(local), "uuid", None)
+        uuid = None if uuid is None else (str(uuid) if str(uuid).startswith("GPU-") else "GPU-" + str(uuid))
+        with ClockSampler(uuid) as clk:
+            lat, arrivals, wall = run_arrivals(srv, jobs, args.serve_rate, seed=args.seed, peaks=peaks)
+        info = srv.query()
+    lat_ms = 1e3 * lat
+    line = {
+        "mode": "serve",
+        "rate_jobs_per_s": args.serve_rate,
+        "seconds": float(arrivals[-1]),
+        "jobs": njobs,
+        "p50_ms": percentile(lat_ms, 50),
+        "p90_ms": percentile(lat_ms, 90),
+        "p99_ms": percentile(lat_ms, 99),
+        "p999_ms": percentile(lat_ms, 99.9),
+        "max_ms": float(np.max(lat_ms)),
+        "mean_ms": float(np.mean(lat_ms)),
+        "offered_gcups": sum(cells) / wall / 1e9,
+        "wall_s": wall,
+        "memory_peak_bytes": peaks.get("bytes_in_use"),
+        "queued_peak_jobs": peaks.get("queued"),
+        "budget_bytes": 40 << 30,
+        "rounds": info["rounds"],
+        "policy": "least remaining work first; jobs older than 500 ms first, in admission order",
+        "workload": "protein families, N ~ U[10,500], root length ~ U[50,1500], Poisson arrivals",
+        "job_generation_s": gen_s,
+    }
+    clocks = clk.summary()
+    if clocks:
+        line["clocks"] = clocks
+    print(json.dumps(line), flush=True)
 
 
 def packed_distmatrix(n, pairs, dist):
@@ -848,6 +947,8 @@ def main():
     args = parse_args()
     if args.impl == "reference":
         reference_arm(args)
+    elif args.serve_only:
+        serve_only(args)
     else:
         ours_arm(args)
 

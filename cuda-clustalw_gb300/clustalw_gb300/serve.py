@@ -120,25 +120,32 @@ def percentile(values, q):
     return float(np.percentile(v, q))
 
 
-def run_arrivals(server, jobs, rate, seed=0):
+def run_arrivals(server, jobs, rate, seed=0, peaks=None):
     """Submit pre-built jobs (list of packed sequence sets) at Poisson times of
     the given rate (jobs/s) while a collector thread waits for, reads and
-    releases finished jobs in completion order. Returns per-job records
-    (arrival offset, latency seconds, n*m cells) and the session wall time."""
+    releases finished jobs in completion order. Returns the per-job latencies
+    (seconds, submission to completion as the server records them), the
+    arrival offsets and the session wall time. If `peaks` is a dict, it
+    receives the largest device memory the admitted jobs held
+    ("bytes_in_use") and the most jobs queued at once ("queued")."""
     rng = np.random.default_rng(seed)
     gaps = rng.exponential(1.0 / rate, size=len(jobs))
     arrivals = np.cumsum(gaps) - gaps[0]
     records = [None] * len(jobs)
     ids = [None] * len(jobs)
+    fresh = []  # job indices submitted since the collector last looked
     submitted = threading.Event()
     lock = threading.Lock()
     errors = []
+    peak = {"bytes_in_use": 0, "queued": 0}
 
     def collector():
         pending = set()
+        last_query = 0.0
         while True:
             with lock:
-                pending |= {k for k, jid in enumerate(ids) if jid is not None and records[k] is None}
+                pending.update(fresh)
+                fresh.clear()
             if not pending and submitted.is_set():
                 break
             done_any = False
@@ -154,6 +161,12 @@ def run_arrivals(server, jobs, rate, seed=0):
                     records[k] = np.array([np.nan] * 4)
                 pending.discard(k)
                 done_any = True
+            now = time.perf_counter()
+            if peaks is not None and now - last_query > 0.05:
+                q = server.query()
+                peak["bytes_in_use"] = max(peak["bytes_in_use"], q["bytes_in_use"])
+                peak["queued"] = max(peak["queued"], q["queued"])
+                last_query = now
             if not done_any:
                 time.sleep(0.001)
 
@@ -167,10 +180,13 @@ def run_arrivals(server, jobs, rate, seed=0):
         jid = server.submit(packed=packed)
         with lock:
             ids[k] = jid
+            fresh.append(k)
     submitted.set()
     th.join()
     wall = time.perf_counter() - t0
     if errors:
         raise errors[0]
+    if peaks is not None:
+        peaks.update(peak)
     lat = np.array([r[3] - r[0] for r in records])
     return lat, arrivals, wall

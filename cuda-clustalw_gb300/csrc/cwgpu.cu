@@ -599,14 +599,22 @@ int gap_extend_of(const cwgpu_params& p) {
 
 size_t block_smem(int K, int warps) { return (size_t)cwgpu::warp_region_bytes(K) * warps; }
 
+// CTAs of k_pairwise<RS> that fit on all SMs at once for an alphabet of K codes.
+template <int RS>
+cudaError_t pair_grid(int K, int sm_count, int* grid) {
+    int per_sm = 0;
+    cudaError_t e = cudaFuncSetAttribute(k_pairwise<RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)block_smem(CWGPU_NUMRES, kWarpsPerBlock));
+    if (e == cudaSuccess)
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise<RS>, kWarpsPerBlock * 32,
+                                                          block_smem(K, kWarpsPerBlock));
+    *grid = (per_sm < 1 ? 1 : per_sm) * sm_count;
+    return e;
+}
+
 template <int RS>
 int persistent_grid(cwgpu_context* ctx, int* grid) {
-    int per_sm = 0;
-    const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
-    CW_CUDA(ctx, cudaFuncSetAttribute(k_pairwise<RS>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)block_smem(CWGPU_NUMRES, kWarpsPerBlock)));
-    CW_CUDA(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise<RS>, kWarpsPerBlock * 32, smem));
-    *grid = (per_sm < 1 ? 1 : per_sm) * ctx->sm_count;
+    CW_CUDA(ctx, pair_grid<RS>(ctx->K, ctx->sm_count, grid));
     return CWGPU_OK;
 }
 
@@ -859,6 +867,36 @@ int check_kernel_error(cwgpu_context* ctx) {
 }  // namespace
 
 int cwgpu_stage_inputs(cwgpu_context* ctx) { return stage_inputs(ctx); }
+
+cudaError_t cwgpu_pair_kernel_grids(int K, int sm_count, int* grid, int* grid_short) {
+    cudaError_t e = pair_grid<cwgpu::kR>(K, sm_count, grid);
+    if (e == cudaSuccess) e = pair_grid<cwgpu::kRShort>(K, sm_count, grid_short);
+    return e;
+}
+
+int cwgpu_pair_kernel_warps_per_cta() { return kWarpsPerBlock; }
+
+cudaError_t cwgpu_enqueue_pair_kernels(const cwgpu::PairArgs& gl, const cwgpu::PairArgs& gs, int grid,
+                                       int grid_short, int prio_high, int prio_low, cudaStream_t s, cudaStream_t s2,
+                                       cudaEvent_t fork, cudaEvent_t join) {
+    const size_t smem = block_smem(gl.K, kWarpsPerBlock);
+    const bool both = gl.npairs > 0 && gs.npairs > 0;
+    cudaError_t e = cudaMemsetAsync(gl.counter, 0, kCounterWords * sizeof(unsigned long long), s);
+    cudaStream_t short_stream = s;
+    if (e == cudaSuccess && both) {
+        e = cudaEventRecord(fork, s);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, fork, 0);
+        short_stream = s2;
+    }
+    if (e == cudaSuccess && gl.npairs > 0) e = launch_persistent<cwgpu::kR>(gl, grid, smem, prio_high, s);
+    if (e == cudaSuccess && gs.npairs > 0)
+        e = launch_persistent<cwgpu::kRShort>(gs, grid_short, smem, prio_low, short_stream);
+    if (e == cudaSuccess && both) {
+        e = cudaEventRecord(join, s2);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(s, join, 0);
+    }
+    return e;
+}
 
 extern "C" {
 

@@ -18,6 +18,20 @@ void cwgpu_fast_release(cwgpu_context* ctx);
 // device arena (one asynchronous copy on ctx->stream); cwgpu.cu.
 int cwgpu_stage_inputs(cwgpu_context* ctx);
 
+// The pair kernels for other callers of the library (the serving engine):
+// persistent grids of the long-pair and short-pair kernels for K codes, and
+// the launch a plan makes over one ordered pair list (gl: its long pairs, on
+// s; gs: its short pairs, on s2 forked from s and joined back; counters of gl
+// reset first, gs.counter = gl.counter + 4). cwgpu.cu.
+namespace cwgpu {
+struct PairArgs;
+}
+cudaError_t cwgpu_pair_kernel_grids(int K, int sm_count, int* grid, int* grid_short);
+int cwgpu_pair_kernel_warps_per_cta();
+cudaError_t cwgpu_enqueue_pair_kernels(const cwgpu::PairArgs& gl, const cwgpu::PairArgs& gs, int grid,
+                                       int grid_short, int prio_high, int prio_low, cudaStream_t s, cudaStream_t s2,
+                                       cudaEvent_t fork, cudaEvent_t join);
+
 struct cwgpu_context {
     int device = 0;
     int sm_count = 0;

@@ -12,15 +12,19 @@
 //   2. forms rounds: a work list of (job, si, sj) items taken from every
 //      admitted job in admission order, longest jobs first within the round,
 //      up to a cell budget per round;
-//   3. runs each round as one persistent launch of k_pairwise_jobs, in which
-//      warps pull items of all the mixed jobs from one queue; two rounds are
-//      in flight on two streams (each with its own scratch rows), so a round
-//      starts filling SMs while the previous one drains, and jobs that arrive
-//      while a round runs join the next one;
+//   3. runs each round as a plan runs a pair list: the round's pairs, longest
+//      first, over a round-local table of the sequences of its jobs, in the
+//      same persistent kernels as cwgpu_align_pairs (k_pairwise, 8 rows per
+//      lane; pairs whose first sequence has at most 128 residues in the 4-row
+//      kernel beside it), then a scatter of the round's distances to the jobs'
+//      result arrays; two rounds are in flight on two streams (each with its
+//      own buffers and scratch rows), so a round starts filling SMs while the
+//      previous one drains, and jobs that arrive while a round runs join the
+//      next one;
 //   4. credits finished pairs to their jobs; a job whose pairs are all done
 //      has its distances copied to host memory and is marked done.
-// Results do not depend on the mix: every pair is computed by the same
-// device code as cwgpu_align_pairs.
+// Results do not depend on the mix: every pair runs the same kernels as
+// cwgpu_align_pairs.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,81 +40,34 @@
 #include <vector>
 
 #include "cwgpu.h"
+#include "cwgpu_context.h"
 #include "cwgpu_device.cuh"
 #include "cwgpu_layout.h"
 
 namespace {
 
-constexpr int kSrvWarpsPerBlock = 4;
+constexpr int kShortRows = 128;  // pairs whose first sequence is this short: the 4-row kernel
 
+// A job's block in the budget arena.
 struct JobDesc {
-    const int8_t* codes;
-    const int64_t* offs;
-    const int32_t* lens;
-    const int32_t* nres;
-    const int32_t* go_table;
+    const int8_t* codes;  // the job's residues in the pair kernels' layout (cwgpu_layout.h)
     float* dist;
     cwgpu_pair_stats* stats;
 };
 
+// Where a round's pair k goes: job slot and pair index q within the job.
 struct WorkItem {
-    int32_t slot, si, sj, q;
+    int32_t slot, q;
 };
 
-struct JobsArgs {
-    const WorkItem* items;
-    long long nitems;
-    const JobDesc* jobs;
-    const int32_t* matrix;
-    int2* scratch;
-    unsigned long long* counter;  // [0] queue head, [1..3] cell counts
-    int* err;
-    int lmax;
-    int ge;
-    int gp1, gp2;
-    int K;
-    int tiny_m, tiny_n;
-};
-
-__global__ void __launch_bounds__(kSrvWarpsPerBlock * 32, 5) k_pairwise_jobs(JobsArgs a) {
-    __shared__ int smat[CWGPU_NUMRES * CWGPU_NUMRES];
-    extern __shared__ __align__(16) uint16_t srv_region[];
-    for (int i = threadIdx.x; i < CWGPU_NUMRES * CWGPU_NUMRES; i += blockDim.x) smat[i] = a.matrix[i];
-    __syncthreads();
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const long long slot = (long long)blockIdx.x * kSrvWarpsPerBlock + warp;
-    cwgpu::Env X;
-    X.smat = smat;
-    X.region = srv_region + (size_t)warp * (cwgpu::warp_region_bytes(a.K) / sizeof(uint16_t));
-    X.K = a.K;
-    X.gp1 = a.gp1;
-    X.gp2 = a.gp2;
-    X.tiny_m = a.tiny_m;
-    X.tiny_n = a.tiny_n;
-    X.err = a.err;
-    int2* bufA = a.scratch + (size_t)slot * 2 * (a.lmax + 1);
-    int2* bufB = bufA + (a.lmax + 1);
-    unsigned long long acc[3] = {0, 0, 0};
-    for (;;) {
-        unsigned long long k = 0;
-        if (lane == 0) k = atomicAdd(a.counter, 1ULL);
-        k = __shfl_sync(cwgpu::kFull, k, 0);
-        if (k >= (unsigned long long)a.nitems) break;
-        const WorkItem it = a.items[k];
-        const JobDesc J = a.jobs[it.slot];
-        const int n = J.lens[it.si], m = J.lens[it.sj];
-        cwgpu_pair_stats st;
-        const float d = cwgpu::align_one(J.codes + J.offs[it.si], n, J.codes + J.offs[it.sj], m, J.nres[it.si],
-                                         J.nres[it.sj], J.go_table[min(n, m)], a.ge, bufA, bufB, X, st, acc);
-        if (lane == 0) {
-            J.dist[it.q] = d;
-            if (J.stats) J.stats[it.q] = st;
-        }
-    }
-    if (lane == 0 && (acc[0] | acc[1] | acc[2])) {
-        atomicAdd(a.counter + 1, acc[0]);
-        atomicAdd(a.counter + 2, acc[1]);
-        atomicAdd(a.counter + 3, acc[2]);
+// Round-local results to the jobs' arrays.
+__global__ void k_scatter(const WorkItem* items, long long n, const JobDesc* jobs, const float* dist,
+                          const cwgpu_pair_stats* stats) {
+    for (long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x; k < n; k += (long long)gridDim.x * blockDim.x) {
+        const WorkItem it = items[k];
+        const JobDesc J = jobs[it.slot];
+        J.dist[it.q] = dist[k];
+        if (J.stats && stats) J.stats[it.q] = stats[k];
     }
 }
 
@@ -189,11 +146,24 @@ struct Job {
     double t_submit = 0, t_admit = 0, t_start = 0, t_done = 0;
 };
 
+// One round in flight: its pair list, sequence table and results, built on the
+// host in a pinned buffer and copied to the device in one piece.
 struct Round {
     std::vector<std::pair<int, int64_t>> credit;  // (slot, pairs)
-    cudaEvent_t ev = nullptr;
+    cudaEvent_t ev = nullptr, fork = nullptr, join = nullptr;
+    cudaStream_t s2 = nullptr;  // the short-pair kernel beside the long-pair one
     bool busy = false;
     int64_t items = 0;
+    unsigned char* h = nullptr;  // pinned
+    size_t cap_h = 0;
+    unsigned char* d = nullptr;
+    size_t cap_d = 0;
+    int64_t n = 0, nlong = 0, nseq = 0;
+    bool stats = false;
+    // byte offsets: pairs at 0, then order, items, sequence offsets, lengths,
+    // residue counts (copied), then distances and statistics (device only)
+    size_t o_order = 0, o_items = 0, o_soffs = 0, o_slens = 0, o_snres = 0, bytes_in = 0, o_dist = 0, o_stats = 0,
+           bytes_all = 0;
 };
 
 }  // namespace
@@ -217,11 +187,11 @@ struct cwgpu_server {
     int* d_err = nullptr;
     cudaStream_t streams[2] = {nullptr, nullptr};
     cudaStream_t upload = nullptr;  // job uploads, waited for before the job's first round
-    WorkItem* d_items[2] = {nullptr, nullptr};
-    WorkItem* h_items[2] = {nullptr, nullptr};  // pinned
     unsigned long long* d_counter[2] = {nullptr, nullptr};
     int2* d_scratch[2] = {nullptr, nullptr};
-    int grid = 0;
+    int32_t* d_go = nullptr;  // gap-open penalty by min(n, m), 0..max_seq_len
+    int grid = 0, grid_short = 0, grid_K = -1;
+    int prio_low = 0, prio_high = 0;
     Round rounds[2];
     int next_round = 0;
     Arena alloc;
@@ -277,8 +247,7 @@ void remap_job(cwgpu_server* s, Job* j, const int8_t* codes, const int64_t* offs
 
 size_t job_bytes(const Job* j) {
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
-    size_t b = up(j->codes.size()) + up(8 * (size_t)j->nseqs) + up(4 * (size_t)j->nseqs) * 2 +
-               up(4 * (size_t)(j->lmax + 1)) + up(4 * (size_t)std::max<int64_t>(j->npairs, 1));
+    size_t b = up(j->codes.size()) + up(4 * (size_t)std::max<int64_t>(j->npairs, 1));
     if (j->want_stats) b += up(sizeof(cwgpu_pair_stats) * (size_t)std::max<int64_t>(j->npairs, 1));
     return b;
 }
@@ -295,26 +264,11 @@ int place_job(cwgpu_server* s, Job* j) {
         return p;
     };
     int8_t* codes = (int8_t*)take(j->codes.size());
-    int64_t* offs = (int64_t*)take(8 * (size_t)j->nseqs);
-    int32_t* lens = (int32_t*)take(4 * (size_t)j->nseqs);
-    int32_t* nres = (int32_t*)take(4 * (size_t)j->nseqs);
-    int32_t* go = (int32_t*)take(4 * (size_t)(j->lmax + 1));
     float* dist = (float*)take(4 * (size_t)std::max<int64_t>(j->npairs, 1));
     cwgpu_pair_stats* stats = j->want_stats ? (cwgpu_pair_stats*)take(sizeof(cwgpu_pair_stats) * j->npairs) : nullptr;
-    std::vector<int32_t> got(j->lmax + 1, 0);
-    for (int L = 1; L <= j->lmax; ++L) {
-        int32_t e = 0;
-        cwgpu_gap_penalties(&s->params, L, L, &got[L], &e);
-    }
     cudaStream_t st = s->upload;
     cudaError_t e = cudaMemcpyAsync(codes, j->codes.data(), j->codes.size(), cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess && j->nseqs) {
-        e = cudaMemcpyAsync(offs, j->offs.data(), 8 * (size_t)j->nseqs, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(lens, j->lens.data(), 4 * (size_t)j->nseqs, cudaMemcpyHostToDevice, st);
-        if (e == cudaSuccess) e = cudaMemcpyAsync(nres, j->nres.data(), 4 * (size_t)j->nseqs, cudaMemcpyHostToDevice, st);
-    }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(go, got.data(), 4 * got.size(), cudaMemcpyHostToDevice, st);
-    j->desc = JobDesc{codes, offs, lens, nres, go, dist, stats};
+    j->desc = JobDesc{codes, dist, stats};
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(s->d_jobs + j->slot, &j->desc, sizeof(JobDesc), cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -339,9 +293,33 @@ void finish_job(cwgpu_server* s, Job* j) {
     s->jobs_done++;
 }
 
-// Items of one round, taken from the admitted jobs in admission order, the
-// longest jobs' items placed first. Returns the number of items.
-int64_t build_round(cwgpu_server* s, Round& r, WorkItem* out) {
+cudaError_t grow_dev(unsigned char*& p, size_t& cap, size_t need) {
+    if (need <= cap && p) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMalloc(&p, need);
+    if (e == cudaSuccess) cap = need;
+    return e;
+}
+
+cudaError_t grow_pinned(unsigned char*& p, size_t& cap, size_t need) {
+    if (need <= cap && p) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    const cudaError_t e = cudaMallocHost(&p, need);
+    if (e == cudaSuccess) cap = need;
+    return e;
+}
+
+// The pairs of one round, taken from the admitted jobs in admission order (or
+// least remaining work first), up to the round's cell budget: a table of the
+// sequences of the round's jobs (offsets into the arena, lengths, residue
+// counts), the pairs as indices into it, where each result goes, and the work
+// order (long pairs first, then short ones, each longest first by n*m, as a
+// plan orders them). Returns the number of pairs, 0 on none, -1 on an error.
+int64_t build_round(cwgpu_server* s, Round& r) {
     r.credit.clear();
     std::vector<Job*> order;
     for (Job* j : s->admitted)
@@ -359,17 +337,22 @@ int64_t build_round(cwgpu_server* s, Round& r, WorkItem* out) {
             return !oa && remaining(a) < remaining(b);
         });
     }
+    struct Take {
+        Job* j;
+        int32_t si0, sj0;
+        int64_t q0, count;
+    };
+    std::vector<Take> taken;
     double budget = s->opts.round_cells;
-    int64_t n = 0;
-    std::vector<std::pair<Job*, std::pair<int64_t, int64_t>>> taken;  // job, [from, to) item range
+    int64_t n = 0, nseq = 0;
+    bool stats = false;
     for (Job* j : order) {
         if (budget <= 0 || n >= s->opts.max_items_per_round) break;
-        const int64_t first = n;
+        Take t{j, j->next_si, j->next_sj, j->scheduled, 0};
         const double per_pair = (double)j->cells_nm / std::max<int64_t>(j->npairs, 1);
-        int64_t q = j->scheduled;
         while (j->scheduled < j->npairs && n < s->opts.max_items_per_round && budget > 0) {
-            out[n++] = WorkItem{j->slot, j->next_si, j->next_sj, (int32_t)q};
-            ++q;
+            ++n;
+            ++t.count;
             ++j->scheduled;
             budget -= per_pair;
             if (++j->next_sj >= j->nseqs) {
@@ -378,44 +361,123 @@ int64_t build_round(cwgpu_server* s, Round& r, WorkItem* out) {
             }
         }
         if (j->t_start == 0) j->t_start = now_s();
-        r.credit.push_back({j->slot, n - first});
-        taken.push_back({j, {first, n}});
+        r.credit.push_back({j->slot, t.count});
+        taken.push_back(t);
+        nseq += j->nseqs;
+        stats |= j->want_stats != 0;
     }
-    // Longest jobs' items first: stable reorder of the per-job ranges.
-    std::stable_sort(taken.begin(), taken.end(), [](const auto& a, const auto& b) { return a.first->lmax > b.first->lmax; });
-    std::vector<WorkItem> tmp(out, out + n);
-    int64_t w = 0;
-    for (auto& t : taken)
-        for (int64_t k = t.second.first; k < t.second.second; ++k) out[w++] = tmp[k];
+    if (n == 0) return 0;
+    auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
+    r.o_order = up(8 * (size_t)n);
+    r.o_items = r.o_order + up(4 * (size_t)n);
+    r.o_soffs = r.o_items + up(sizeof(WorkItem) * (size_t)n);
+    r.o_slens = r.o_soffs + up(8 * (size_t)nseq);
+    r.o_snres = r.o_slens + up(4 * (size_t)nseq);
+    r.bytes_in = r.o_snres + up(4 * (size_t)nseq);
+    r.o_dist = r.bytes_in;
+    r.o_stats = r.o_dist + up(4 * (size_t)n);
+    r.bytes_all = r.o_stats + (stats ? sizeof(cwgpu_pair_stats) * (size_t)n : 0);
+    if (grow_pinned(r.h, r.cap_h, r.bytes_in) != cudaSuccess || grow_dev(r.d, r.cap_d, r.bytes_all) != cudaSuccess)
+        return -1;
+    int32_t* pairs = reinterpret_cast<int32_t*>(r.h);
+    int32_t* ord = reinterpret_cast<int32_t*>(r.h + r.o_order);
+    WorkItem* items = reinterpret_cast<WorkItem*>(r.h + r.o_items);
+    int64_t* soffs = reinterpret_cast<int64_t*>(r.h + r.o_soffs);
+    int32_t* slens = reinterpret_cast<int32_t*>(r.h + r.o_slens);
+    int32_t* snres = reinterpret_cast<int32_t*>(r.h + r.o_snres);
+    // Sort keys as in a plan's work order: the top 12 bits of n*m as a float,
+    // long pairs (first sequence longer than kShortRows) before short ones.
+    constexpr int kKeyBits = 12, kBuckets = 1 << kKeyBits;
+    std::vector<uint16_t> key((size_t)n);
+    std::vector<int64_t> start(2 * kBuckets + 1, 0);
+    int64_t k = 0, base = 0;
+    for (const Take& t : taken) {
+        const Job* j = t.j;
+        const int64_t codes_off = (int64_t)(j->desc.codes - reinterpret_cast<const int8_t*>(s->arena));
+        for (int i = 0; i < j->nseqs; ++i) {
+            soffs[base + i] = codes_off + j->offs[i];
+            slens[base + i] = j->lens[i];
+            snres[base + i] = j->nres[i];
+        }
+        int32_t si = t.si0, sj = t.sj0;
+        for (int64_t c = 0; c < t.count; ++c, ++k) {
+            pairs[2 * k] = (int32_t)(base + si);
+            pairs[2 * k + 1] = (int32_t)(base + sj);
+            items[k] = WorkItem{j->slot, (int32_t)(t.q0 + c)};
+            const float w = (float)((double)j->lens[si] * (double)j->lens[sj]);
+            uint32_t bits;
+            memcpy(&bits, &w, sizeof(bits));
+            const int b = (j->lens[si] <= kShortRows ? kBuckets : 0) + (kBuckets - 1 - (int)(bits >> (31 - kKeyBits)));
+            key[(size_t)k] = (uint16_t)b;
+            ++start[b + 1];
+            if (++sj >= j->nseqs) {
+                ++si;
+                sj = si + 1;
+            }
+        }
+        base += j->nseqs;
+    }
+    for (int b = 0; b < 2 * kBuckets; ++b) start[b + 1] += start[b];
+    r.nlong = start[kBuckets];
+    for (int64_t q = 0; q < n; ++q) ord[start[key[(size_t)q]]++] = (int32_t)q;
+    r.n = n;
+    r.nseq = nseq;
+    r.stats = stats;
     return n;
 }
 
 int launch_round(cwgpu_server* s, int ri, int64_t nitems) {
     Round& r = s->rounds[ri];
     cudaStream_t st = s->streams[ri];
-    cudaError_t e = cudaMemcpyAsync(s->d_items[ri], s->h_items[ri], sizeof(WorkItem) * nitems, cudaMemcpyHostToDevice, st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(s->d_counter[ri], 0, 4 * sizeof(unsigned long long), st);
+    cudaError_t e = cudaSuccess;
+    const int K = std::max(1, s->K);
+    if (s->grid_K != K) {
+        e = cwgpu_pair_kernel_grids(K, s->sm_count, &s->grid, &s->grid_short);
+        // the scratch holds rows for 5 CTAs per SM of each kernel (their launch bound)
+        s->grid = std::min(s->grid, 5 * s->sm_count);
+        s->grid_short = std::min(s->grid_short, 5 * s->sm_count);
+        s->grid_K = K;
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(r.d, r.h, r.bytes_in, cudaMemcpyHostToDevice, st);
     if (e == cudaSuccess) {
-        JobsArgs a;
-        a.items = s->d_items[ri];
-        a.nitems = nitems;
-        a.jobs = s->d_jobs;
-        a.matrix = s->d_matrix;
-        a.scratch = s->d_scratch[ri];
-        a.counter = s->d_counter[ri];
-        a.err = s->d_err;
-        a.lmax = s->opts.max_seq_len;
-        a.ge = s->ge;
+        const int wpc = cwgpu_pair_kernel_warps_per_cta();
+        cwgpu::PairArgs gl;
+        gl.codes = reinterpret_cast<const int8_t*>(s->arena);
+        gl.offs = reinterpret_cast<const int64_t*>(r.d + r.o_soffs);
+        gl.lens = reinterpret_cast<const int32_t*>(r.d + r.o_slens);
+        gl.nres = reinterpret_cast<const int32_t*>(r.d + r.o_snres);
+        gl.pairs = reinterpret_cast<const int32_t*>(r.d);
+        gl.order = reinterpret_cast<const int32_t*>(r.d + r.o_order);
+        gl.go_table = s->d_go;
+        gl.matrix = s->d_matrix;
+        gl.dist = reinterpret_cast<float*>(r.d + r.o_dist);
+        gl.stats = r.stats ? reinterpret_cast<cwgpu_pair_stats*>(r.d + r.o_stats) : nullptr;
+        gl.scratch = s->d_scratch[ri];
+        gl.counter = s->d_counter[ri];
+        gl.err = s->d_err;
+        gl.cells = s->d_counter[ri] + 1;
+        gl.npairs = r.nlong;
+        gl.lmax = s->opts.max_seq_len;
+        gl.ge = s->ge;
         const int gp1 = s->params.gap_pos1, gp2 = s->params.gap_pos2;
-        a.gp1 = (gp1 >= 0 && gp1 < CWGPU_NUMRES) ? s->dense_of[gp1] : -1;
-        a.gp2 = (gp2 >= 0 && gp2 < CWGPU_NUMRES) ? s->dense_of[gp2] : -1;
-        a.K = std::max(1, s->K);
-        a.tiny_m = 32;
-        a.tiny_n = cwgpu::kTinyMaxN;
-        const size_t smem = (size_t)cwgpu::warp_region_bytes(a.K) * kSrvWarpsPerBlock;
-        const long long want = (nitems + kSrvWarpsPerBlock - 1) / kSrvWarpsPerBlock;
-        const int grid = (int)std::min<long long>(s->grid, want);
-        k_pairwise_jobs<<<grid, kSrvWarpsPerBlock * 32, smem, st>>>(a);
+        gl.gp1 = (gp1 >= 0 && gp1 < CWGPU_NUMRES) ? s->dense_of[gp1] : -1;
+        gl.gp2 = (gp2 >= 0 && gp2 < CWGPU_NUMRES) ? s->dense_of[gp2] : -1;
+        gl.K = K;
+        gl.tiny_m = 32;
+        gl.tiny_n = cwgpu::kTinyMaxN;
+        cwgpu::PairArgs gs = gl;
+        gs.order = gl.order + r.nlong;
+        gs.npairs = r.n - r.nlong;
+        gs.counter = s->d_counter[ri] + 4;
+        if (r.nlong > 0) gs.scratch += (size_t)5 * s->sm_count * wpc * 2 * (size_t)(s->opts.max_seq_len + 1);
+        e = cwgpu_enqueue_pair_kernels(gl, gs, s->grid, s->grid_short, s->prio_high, s->prio_low, st, r.s2, r.fork,
+                                       r.join);
+    }
+    if (e == cudaSuccess) {
+        const int blocks = (int)std::min<int64_t>((r.n + 255) / 256, 4 * (int64_t)s->sm_count);
+        k_scatter<<<blocks, 256, 0, st>>>(reinterpret_cast<const WorkItem*>(r.d + r.o_items), r.n, s->d_jobs,
+                                          reinterpret_cast<const float*>(r.d + r.o_dist),
+                                          r.stats ? reinterpret_cast<const cwgpu_pair_stats*>(r.d + r.o_stats) : nullptr);
         e = cudaGetLastError();
     }
     if (e == cudaSuccess) e = cudaEventRecord(r.ev, st);
@@ -481,7 +543,12 @@ void scheduler(cwgpu_server* s) {
                 if (s->rounds[0].busy || s->rounds[1].busy) break;
                 upload_matrix(s);
             }
-            const int64_t n = build_round(s, s->rounds[ri], s->h_items[ri]);
+            const int64_t n = build_round(s, s->rounds[ri]);
+            if (n < 0) {
+                s->fatal = CWGPU_ERR_OOM;
+                s->error = "round buffers: allocation failed";
+                break;
+            }
             if (n == 0) break;
             if (launch_round(s, ri, n)) {
                 s->fatal = CWGPU_ERR_CUDA;
@@ -560,23 +627,27 @@ int cwgpu_server_create(int device, const int32_t* matrix, const cwgpu_params* p
     if (e == cudaSuccess) e = cudaMalloc(&s->d_matrix, sizeof(int32_t) * CWGPU_NUMRES * CWGPU_NUMRES);
     if (e == cudaSuccess) e = cudaMalloc(&s->d_err, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(s->d_err, 0, sizeof(int));
-    int per_sm = 0;
-    const size_t smem_max = (size_t)cwgpu::warp_region_bytes(CWGPU_NUMRES) * kSrvWarpsPerBlock;
-    if (e == cudaSuccess)
-        e = cudaFuncSetAttribute(k_pairwise_jobs, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_max);
-    if (e == cudaSuccess)
-        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_pairwise_jobs, kSrvWarpsPerBlock * 32,
-                                                          (size_t)cwgpu::warp_region_bytes(20) * kSrvWarpsPerBlock);
-    s->grid = std::max(1, per_sm) * s->sm_count;
+    if (e == cudaSuccess) e = cudaDeviceGetStreamPriorityRange(&s->prio_low, &s->prio_high);
+    if (e == cudaSuccess) e = cudaMalloc(&s->d_go, sizeof(int32_t) * (size_t)(opts->max_seq_len + 1));
+    if (e == cudaSuccess) {
+        std::vector<int32_t> got((size_t)opts->max_seq_len + 1, 0);
+        for (int L = 1; L <= opts->max_seq_len; ++L) {
+            int32_t ge = 0;
+            cwgpu_gap_penalties(params, L, L, &got[(size_t)L], &ge);
+        }
+        e = cudaMemcpy(s->d_go, got.data(), sizeof(int32_t) * got.size(), cudaMemcpyHostToDevice);
+    }
+    // Scratch rows per round: 5 CTAs per SM of each pair kernel (their launch bound).
+    const size_t slots = (size_t)2 * 5 * s->sm_count * cwgpu_pair_kernel_warps_per_cta();
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->upload, cudaStreamNonBlocking);
     for (int i = 0; i < 2 && e == cudaSuccess; ++i) {
         e = cudaStreamCreateWithFlags(&s->streams[i], cudaStreamNonBlocking);
-        if (e == cudaSuccess) e = cudaMalloc(&s->d_items[i], sizeof(WorkItem) * opts->max_items_per_round);
-        if (e == cudaSuccess) e = cudaMallocHost(&s->h_items[i], sizeof(WorkItem) * opts->max_items_per_round);
-        if (e == cudaSuccess) e = cudaMalloc(&s->d_counter[i], 4 * sizeof(unsigned long long));
-        if (e == cudaSuccess)
-            e = cudaMalloc(&s->d_scratch[i], (size_t)s->grid * kSrvWarpsPerBlock * 2 * (opts->max_seq_len + 1) * sizeof(int2));
+        if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->rounds[i].s2, cudaStreamNonBlocking);
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_counter[i], 8 * sizeof(unsigned long long));
+        if (e == cudaSuccess) e = cudaMalloc(&s->d_scratch[i], slots * 2 * (opts->max_seq_len + 1) * sizeof(int2));
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->rounds[i].ev, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->rounds[i].fork, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&s->rounds[i].join, cudaEventDisableTiming);
     }
     if (e != cudaSuccess) {
         cwgpu_server_destroy(s);
@@ -607,9 +678,13 @@ void cwgpu_server_destroy(cwgpu_server* s) {
     cudaSetDevice(s->device);
     for (int i = 0; i < 2; ++i) {
         if (s->streams[i]) cudaStreamSynchronize(s->streams[i]);
-        if (s->rounds[i].ev) cudaEventDestroy(s->rounds[i].ev);
-        if (s->d_items[i]) cudaFree(s->d_items[i]);
-        if (s->h_items[i]) cudaFreeHost(s->h_items[i]);
+        Round& r = s->rounds[i];
+        if (r.ev) cudaEventDestroy(r.ev);
+        if (r.fork) cudaEventDestroy(r.fork);
+        if (r.join) cudaEventDestroy(r.join);
+        if (r.s2) cudaStreamDestroy(r.s2);
+        if (r.h) cudaFreeHost(r.h);
+        if (r.d) cudaFree(r.d);
         if (s->d_counter[i]) cudaFree(s->d_counter[i]);
         if (s->d_scratch[i]) cudaFree(s->d_scratch[i]);
         if (s->streams[i]) cudaStreamDestroy(s->streams[i]);
@@ -618,6 +693,7 @@ void cwgpu_server_destroy(cwgpu_server* s) {
     if (s->arena) cudaFree(s->arena);
     if (s->d_jobs) cudaFree(s->d_jobs);
     if (s->d_matrix) cudaFree(s->d_matrix);
+    if (s->d_go) cudaFree(s->d_go);
     if (s->d_err) cudaFree(s->d_err);
     for (auto& kv : s->jobs) delete kv.second;
     delete s;

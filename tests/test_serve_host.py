@@ -44,6 +44,11 @@ class FakeServer:
         with self.lock:
             self.released.append(job_id)
 
+    def query(self):
+        with self.lock:  # bytes held: 1 MiB per job submitted and not released
+            live = len(self.submitted) - len(self.released)
+        return dict(queued=0, bytes_in_use=live << 20)
+
 
 def test_run_arrivals_reads_and_releases_every_job():
     from clustalw_gb300.serve import run_arrivals
@@ -74,3 +79,14 @@ def test_percentile():
     assert math.isnan(percentile([], 50))
     assert percentile([4, 1, 3, 2], 50) == 2.5
     assert percentile(range(101), 99) == 99.0
+
+
+def test_run_arrivals_records_the_memory_peak():
+    from clustalw_gb300.serve import run_arrivals
+
+    srv = FakeServer(service_s=0.12)
+    peaks = {}
+    lat, _, _ = run_arrivals(srv, [None] * 12, rate=400.0, seed=5, peaks=peaks)
+    assert len(lat) == 12 and sorted(srv.released) == sorted(srv.submitted)
+    # all 12 jobs arrive within about 30 ms and each is held 120 ms
+    assert peaks["bytes_in_use"] >= 8 << 20 and peaks["queued"] == 0
