@@ -1,7 +1,9 @@
 """Multi-GPU sharding logic on CPU: the static partition covers every pair
 once with balanced n*m, and two gloo ranks assemble exactly the distances one
-process would produce. The per-rank compute here is a deterministic stand-in
-(no GPU on this host); the GPU path itself is covered by the -m gpu tests."""
+process would produce, with the oracle (the CPU restatement of the full
+pairwise stage, and of the quick k-tuple distances) as each rank's aligner,
+since this host has no GPU; the GPU path itself is covered by the -m gpu
+tests."""
 import os
 
 import numpy as np
@@ -9,10 +11,19 @@ import torch.distributed as dist
 import torch.multiprocessing as mp
 
 
-def fake_align(seqs, pairs):
-    lens = np.array([len(s) for s in seqs])
-    p = np.asarray(pairs).reshape(-1, 2)
-    return (lens[p[:, 0]] * 7 + lens[p[:, 1]] * 13 + p[:, 0] * 3 + p[:, 1]).astype(np.float32)
+def full_align(seqs, pairs):
+    """Full pairwise distances (float32) from the oracle, Gonnet at 10 / 0.1."""
+    from clustalw_gb300 import load_matrix
+    from oracle import oracle
+
+    matrix, params = load_matrix("protein")
+    return oracle.align_pairs(seqs, matrix, params, pairs, nthreads=1)["dist"]
+
+
+def _seqs_full():
+    from clustalw_gb300.synth import protein_family
+
+    return protein_family(18, 70, 4) + protein_family(19, 140, 5)
 
 
 def test_partition_covers_and_balances():
@@ -34,13 +45,15 @@ def test_partition_covers_and_balances():
 def _rank_main(rank, world, port, out_path):
     os.environ["MASTER_ADDR"] = "127.0.0.1"
     os.environ["MASTER_PORT"] = str(port)
+    import sys
+
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
     dist.init_process_group("gloo", rank=rank, world_size=world)
     from clustalw_gb300.shard import sharded_pairwise
     from clustalw_gb300.synth import all_pairs
 
-    rng = np.random.default_rng(1)
-    seqs = [np.zeros(int(L), np.int8) for L in rng.integers(5, 400, size=37)]
-    res = sharded_pairwise(seqs, all_pairs(37), fake_align, group=dist.group.WORLD)
+    seqs = _seqs_full()
+    res = sharded_pairwise(seqs, all_pairs(37), full_align, group=dist.group.WORLD)
     if rank == 0:
         np.save(out_path, res)
     else:
@@ -58,10 +71,10 @@ def test_two_gloo_ranks_assemble_the_full_result(tmp_path):
         port = s.getsockname()[1]
     out = str(tmp_path / "d.npy")
     mp.spawn(_rank_main, args=(2, port, out), nprocs=2, join=True)
-    rng = np.random.default_rng(1)
-    seqs = [np.zeros(int(L), np.int8) for L in rng.integers(5, 400, size=37)]
-    want = fake_align(seqs, all_pairs(37))
-    assert np.array_equal(np.load(out), want)
+    want = full_align(_seqs_full(), all_pairs(37))
+    got = np.load(out)
+    assert got.dtype == np.float32
+    assert np.array_equal(got.view(np.int32), want.view(np.int32))
 
 
 def quick_align(seqs, pairs):
