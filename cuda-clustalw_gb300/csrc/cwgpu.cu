@@ -92,8 +92,8 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
 // all nw warps, whose results are reduced across the warps; Myers-Miller
 // frames of at least large_rows rows are divided by the two halves of the CTA
 // at once (forward half on warps [0, nw/2), reverse half on [nw/2, nw)), and
-// the smaller frames they leave are shared out, one whole frame subtree per
-// warp (cwgpu::mm_align). Frames are independent once (A, B, M, N, tb, te) are
+// the smaller frames they leave go to a shared stack that every warp takes
+// frames from (cwgpu::mm_align) and gives the children it makes back to. Frames are independent once (A, B, M, N, tb, te) are
 // known and diff()'s identity and match counts are sums over its M == 1
 // leaves, so results equal those of the one-warp form.
 constexpr int kCtaMaxWarps = 16;
@@ -112,6 +112,7 @@ struct CtaCtl {
     int ident[kCtaMaxWarps], match[kCtaMaxWarps];
     int mm;  // diff()'s score of the pair
     int nstack, nsmall, small_next;
+    int lock, active;  // the shared frame stack `small`: its lock, warps holding a frame from it
     int4 stack[kCtaStack];  // large frames: (A, B, M | root, N | tb << 29 | te << 30)
     int4 small[kCtaSmall];  // frames for one warp each
 };
@@ -137,29 +138,92 @@ __device__ __forceinline__ cwgpu::Best cta_reduce(const CtaCtl& C, int nw) {
 
 __device__ __forceinline__ bool cta_large(int M, int N, int large_rows) { return M >= large_rows && N >= 64; }
 
-// The small frames of C.small, one per warp at a time (every thread calls).
+constexpr int kShareRows = 64;  // frames with fewer rows stay with the warp that divided them
+
+// The frames of C.small (every thread calls). C.small is a stack that every
+// warp takes frames from and gives frames to: a warp takes a frame, runs the
+// one-warp Myers-Miller on it, and after each division gives the right child
+// back to the stack (if it has kShareRows rows or more and there is room) so
+// that idle warps can take it. The phase ends when the stack is empty and no
+// warp holds a frame. A warp that finds the stack empty while others still
+// hold frames waits (bounded, like the stripe hand-overs).
 template <int RS>
 __device__ void cta_small_frames(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, const int8_t* s2,
                                  const int8_t* s2r, int m, int go, int ge, int2* bufA, int2* bufB, const cwgpu::Env& X,
-                                 int& ident, int& match, long long& cells) {
+                                 const CtaArgs& ca, int& ident, int& match, long long& cells) {
     const int lane = threadIdx.x & 31;
-    if (threadIdx.x == 0) C.small_next = 0;
+    if (threadIdx.x == 0) {
+        C.active = 0;
+        C.lock = 0;
+    }
     __syncthreads();
-    const int nsmall = C.nsmall;
+    cwgpu::FrameShare fs;
+    fs.frames = C.small;
+    fs.count = &C.nsmall;
+    fs.lock = &C.lock;
+    fs.cap = kCtaSmall;
+    fs.min_rows = kShareRows;
+    volatile int* vcount = &C.nsmall;
+    volatile int* vactive = &C.active;
+    volatile int* vabort = &C.abort;
+    unsigned long long t_wait = 0;
     for (;;) {
-        int k = 0;
-        if (lane == 0) k = atomicAdd(&C.small_next, 1);
-        k = __shfl_sync(cwgpu::kFull, k, 0);
-        if (k >= nsmall) break;
-        const int4 F = C.small[k];
+        int state = 0;  // 0: nothing to take yet, 1: took a frame, 2: phase over
+        int fa = 0, fb = 0, fm = 0, fn = 0;
+        if (lane == 0) {
+            if (*vabort) {
+                state = 2;
+            } else if (atomicCAS(&C.lock, 0, 1) == 0) {
+                __threadfence_block();
+                const int c = *vcount;
+                if (c > 0) {
+                    volatile int* e = reinterpret_cast<volatile int*>(&C.small[c - 1]);
+                    fa = e[0];
+                    fb = e[1];
+                    fm = e[2];
+                    fn = e[3];
+                    *vcount = c - 1;
+                    atomicAdd(&C.active, 1);
+                    state = 1;
+                } else if (*vactive == 0) {
+                    state = 2;
+                }
+                __threadfence_block();
+                atomicExch(&C.lock, 0);
+            }
+            if (state == 0) {  // bounded wait for frames other warps still hold
+                const unsigned long long now = cwgpu::global_ns();
+                if (t_wait == 0) {
+                    t_wait = now;
+                } else if (now - t_wait > ca.limit_ns) {
+                    *vabort = 1;
+                    atomicExch(X.err, cwgpu::kStatusTimeout);
+                    state = 2;
+                }
+            } else {
+                t_wait = 0;
+            }
+        }
+        state = __shfl_sync(cwgpu::kFull, state, 0);
+        if (state == 2) break;
+        if (state == 0) continue;
+        fa = __shfl_sync(cwgpu::kFull, fa, 0);
+        fb = __shfl_sync(cwgpu::kFull, fb, 0);
+        fm = __shfl_sync(cwgpu::kFull, fm, 0);
+        fn = __shfl_sync(cwgpu::kFull, fn, 0);
         int mmf = 0, id = 0, mt = 0;
         long long ce = 0;
-        cwgpu::mm_align<RS>(s1, s1r, n, s2, s2r, m, F.x, F.y, F.z & ~kRootBit, F.w, go, ge, bufA, bufB, X, mmf, id, mt,
-                            ce);
+        cwgpu::mm_align<RS, true, true>(s1, s1r, n, s2, s2r, m, fa, fb, fm & ~kRootBit, fn, go, ge, bufA, bufB, X, mmf,
+                                        id, mt, ce, &fs);
         ident += id;
         match += mt;
         cells += ce;
-        if ((F.z & kRootBit) && lane == 0) C.mm = mmf;
+        if ((fm & kRootBit) && lane == 0) C.mm = mmf;
+        __syncwarp();
+        if (lane == 0) {
+            __threadfence_block();
+            atomicSub(&C.active, 1);  // after every frame this one gave to the stack
+        }
     }
     __syncthreads();
     if (threadIdx.x == 0) C.nsmall = 0;
@@ -251,9 +315,9 @@ __device__ void cta_diff(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, 
         }
         __syncthreads();
         if (C.nsmall > kCtaSmall - 2)
-            cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ident, match, ncell);
+            cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ca, ident, match, ncell);
     }
-    cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ident, match, ncell);
+    cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ca, ident, match, ncell);
     if (lane == 0) {
         C.ident[warp] = ident;
         C.match[warp] = match;

@@ -712,6 +712,39 @@ static __device__ int lane_mm(const int8_t* s1, const int8_t* s2, int A0, int B0
 
 // ---------------------------------------------------------------- diff()
 
+// A CTA's shared stack of Myers-Miller frames (used by the one-CTA-per-pair
+// kernel): frames (A, B, M, N | tb << 29 | te << 30) that any warp of the CTA
+// may take; count and lock live in shared memory, the lock taken by one lane.
+struct FrameShare {
+    int4* frames;
+    volatile int* count;
+    int* lock;
+    int cap;
+    int min_rows;  // frames with fewer rows stay with the warp that made them
+};
+
+// Lane 0: pushes f if the stack has room and its lock is free within a few
+// tries; returns whether it did (else the caller keeps the frame).
+__device__ __forceinline__ bool share_push(const FrameShare& fs, int4 f) {
+    for (int tries = 0; tries < 64; ++tries) {
+        if (atomicCAS(fs.lock, 0, 1) == 0) {
+            __threadfence_block();
+            bool ok = false;
+            const int c = *fs.count;
+            if (c < fs.cap) {
+                fs.frames[c] = f;
+                __threadfence_block();
+                *fs.count = c + 1;
+                ok = true;
+            }
+            __threadfence_block();
+            atomicExch(fs.lock, 0);
+            return ok;
+        }
+    }
+    return false;
+}
+
 // Midpoint scans of a Myers-Miller frame (FullPairwiseAlign.cpp:570-593), by
 // one warp. fwd[j] holds (HH, DD + goe) of row midi from the forward half,
 // rev[N - j] holds (RR, SS + goe) of the same row from the reverse half (j =
@@ -784,11 +817,14 @@ __device__ __forceinline__ void midpoint_scan(const int2* fwd, const int2* rev, 
 // seq1[A + i] is s1[A + i - 1]. s1r/s2r are the reversed copies of the n- and
 // m-residue sequences (s1r[i] = s1[n - 1 - i]), which the reverse halves read.
 // N0 carries the top frame's flags: tb = gapOpen if bit 29, te if bit 30 (a
-// whole pair's frame has neither).
-template <int RS, bool NC = true>
+// whole pair's frame has neither). SHARE: after each division the right child,
+// if it has at least fs->min_rows rows, goes to the CTA's shared stack (when
+// it has room) for any warp of the CTA to take, instead of this warp's own.
+template <int RS, bool NC = true, bool SHARE = false>
 static __device__ void mm_align(const int8_t* s1, const int8_t* s1r, int n, const int8_t* s2, const int8_t* s2r, int m,
                                 int A0, int B0, int M0, int N0, int go, int ge, int2* bufA, int2* bufB, const Env& X,
-                                int& mm_score, int& n_ident, int& n_match, long long& cells) {
+                                int& mm_score, int& n_ident, int& n_match, long long& cells,
+                                const FrameShare* fs = nullptr) {
     const int lane = threadIdx.x & 31;
     constexpr int NMASK = (1 << 29) - 1;
     int stA = 0, stB = 0, stM = 0, stN = 0;  // stack entry `lane`
@@ -925,6 +961,22 @@ static __device__ void mm_align(const int8_t* s1, const int8_t* s1r, int n, cons
         if (sp + 2 > 32) {
             if (lane == 0) atomicExch(X.err, 1);
             break;
+        }
+        if constexpr (SHARE) {
+            const int4 right = !type2 ? make_int4(A + midi, B + midj, M - midi, (N - midj) | (1 << 29) | (tef << 30))
+                                      : make_int4(A + midi + 1, B + midj, M - midi - 1, (N - midj) | (tef << 30));
+            int shared = 0;
+            if (lane == 0 && right.z >= fs->min_rows) shared = share_push(*fs, right) ? 1 : 0;
+            if (__shfl_sync(kFull, shared, 0)) {
+                if (lane == sp) {
+                    stA = A;
+                    stB = B;
+                    stM = !type2 ? midi : midi - 1;
+                    stN = !type2 ? (midj | (tbf << 29) | (1 << 30)) : (midj | (tbf << 29));
+                }
+                sp += 1;
+                continue;
+            }
         }
         if (!type2) {
             if (lane == sp) {

@@ -108,7 +108,7 @@ def test_one_column_call_takes_the_cta_form_by_default(ctx):
     n = len(g["seqs"])
     pairs = range_pairs(n, 0, n, n - 2, n)
     assert len(pairs) == n - 1
-    assert ctx.get_cta_tuning() == (-1, 0, 512)  # defaults: automatic threshold and warps
+    assert ctx.get_cta_tuning() == (-1, 0, 1024)  # defaults: automatic threshold and warps
     plan = ctx.plan(pairs)
     assert plan.pair_ctas()
     plan.close()
