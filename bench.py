@@ -765,8 +765,11 @@ def ours_arm(args):
         from clustalw_gb300 import autotune
 
         choice, timings = autotune.tune(ctx, packed[2], pairs, gpu_name=torch.cuda.get_device_name(local))
+        cta_choice, cta_timings = autotune.tune_cta(ctx, packed[2], pairs)
         tuning = {"tiny_m_tiny_n_short_rows": list(choice), "autotuned": True,
-                  "candidates_s": {",".join(map(str, c)): round(t, 4) for c, t in timings.items()}}
+                  "candidates_s": {",".join(map(str, c)): round(t, 4) for c, t in timings.items()},
+                  "cta_max_pairs_warps_large_rows": list(cta_choice),
+                  "cta_candidates_s": {",".join(map(str, c)): round(t, 4) for c, t in cta_timings.items()}}
     plan = ctx.plan(pairs)
     # A dedicated stream: the graph is launched on it and the CUDA events are
     # recorded on it (torch's default stream has handle 0, which the C ABI
