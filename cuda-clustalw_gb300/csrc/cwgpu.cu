@@ -885,10 +885,12 @@ bool use_cta(const cwgpu_context* ctx, int64_t nlong) {
 // drains. Long pairs run one CTA per pair when there are at most cta_pairs of
 // them, else one warp per pair. Works the same under stream capture.
 cudaError_t enqueue_pairs(cwgpu_context* ctx, const cwgpu::PairArgs& gl, const cwgpu::PairArgs& gs, cudaStream_t s,
-                          cudaStream_t s2, cudaEvent_t fork, cudaEvent_t join) {
+                          cudaStream_t s2, cudaEvent_t fork, cudaEvent_t join, bool counters_zeroed = false) {
     const size_t smem = block_smem(ctx->K, kWarpsPerBlock);
     const bool both = gl.npairs > 0 && gs.npairs > 0;
-    cudaError_t e = cudaMemsetAsync(ctx->d_counter, 0, kCounterWords * sizeof(unsigned long long), s);
+    cudaError_t e = counters_zeroed
+                        ? cudaSuccess
+                        : cudaMemsetAsync(gl.counter, 0, kCounterWords * sizeof(unsigned long long), s);
     cudaStream_t short_stream = s;
     if (e == cudaSuccess && both) {
         e = cudaEventRecord(fork, s);
@@ -914,6 +916,12 @@ void split_args(cwgpu_context* ctx, const int32_t* d_pairs, const int32_t* d_ord
     *gs = make_args(ctx, d_pairs, d_order + nlong, npairs - nlong, d_dist, d_stats);
     gs->counter = ctx->d_counter + 4;
     if (nlong > 0) gs->scratch += (size_t)ctx->grid * kWarpsPerBlock * 2 * (size_t)(ctx->lmax + 1);
+}
+
+int status_error(cwgpu_context* ctx, int err) {
+    if (err == cwgpu::kStatusTimeout)
+        return fail(ctx, CWGPU_ERR_TIMEOUT, "a hand-over wait between the warps of a pair's CTA timed out");
+    return fail(ctx, CWGPU_ERR_DEVICE, "kernel reported an internal limit (Myers-Miller stack depth)");
 }
 
 int check_kernel_error(cwgpu_context* ctx) {
@@ -1046,10 +1054,7 @@ void cwgpu_destroy(cwgpu_context* ctx) {
     dfree(ctx->d_scratch);
     dfree(ctx->d_counter);
     dfree(ctx->d_err);
-    dfree(ctx->d_pairs1);
-    dfree(ctx->d_order1);
-    dfree(ctx->d_dist1);
-    dfree(ctx->d_stats1);
+    dfree(ctx->d_call);
     if (ctx->stream_short) cudaStreamSynchronize(ctx->stream_short);
     if (ctx->ev_fork) cudaEventDestroy(ctx->ev_fork);
     if (ctx->ev_join) cudaEventDestroy(ctx->ev_join);
@@ -1262,50 +1267,58 @@ int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
     if (rc) return rc;
     if (npairs == 0) return CWGPU_OK;
     CW_CUDA(ctx, cudaSetDevice(ctx->device));
-    if (npairs > ctx->cap_pairs1) {
-        int64_t c1 = 0, c2 = 0, c3 = 0, c4 = 0;
-        ctx->cap_pairs1 = 0;
-        CW_CUDA(ctx, grow(ctx->d_pairs1, c1, 2 * npairs));
-        CW_CUDA(ctx, grow(ctx->d_order1, c2, npairs));
-        CW_CUDA(ctx, grow(ctx->d_dist1, c3, npairs));
-        CW_CUDA(ctx, grow(ctx->d_stats1, c4, npairs));
-        ctx->cap_pairs1 = npairs;
-    }
     // Created on first use; each handle on its own, so a call after a failed
     // creation retries what is missing.
     if (!ctx->stream_short) CW_CUDA(ctx, cudaStreamCreateWithFlags(&ctx->stream_short, cudaStreamNonBlocking));
     if (!ctx->ev_fork) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_fork, cudaEventDisableTiming));
     if (!ctx->ev_join) CW_CUDA(ctx, cudaEventCreateWithFlags(&ctx->ev_join, cudaEventDisableTiming));
-    // Pair list and work order in, distances, statistics and the status word
-    // out, all through one pinned buffer: asynchronous copies on the stream
-    // and a single synchronization at the end.
+    // One buffer per call, filled and read back in one copy each way:
+    //   in:  pair list, work order, zeroed queue counters, zeroed status word
+    //   out: status word and distances (the statistics, if asked for, after them)
     auto up = [](size_t b) { return (b + 255) & ~(size_t)255; };
     const size_t n = (size_t)npairs;
-    const size_t o_order = up(8 * n), o_dist = o_order + up(4 * n);
-    const size_t o_stats = o_dist + up(4 * n), o_err = o_stats + up(sizeof(cwgpu_pair_stats) * n);
-    CW_CUDA(ctx, pinned_grow(ctx->h_io, ctx->cap_h_io, o_err + 4));
+    const size_t o_order = up(8 * n), o_ctr = o_order + up(4 * n), o_err = o_ctr + 256;
+    const size_t o_dist = o_err + 16, o_stats = up(o_dist + 4 * n);
+    const size_t bytes_in = o_err + 16, bytes_out = 16 + 4 * n;
+    const size_t total = o_stats + sizeof(cwgpu_pair_stats) * n;
+    if (total > ctx->cap_call) {
+        dfree(ctx->d_call);
+        ctx->cap_call = 0;
+        CW_CUDA(ctx, cudaMalloc(&ctx->d_call, total));
+        ctx->cap_call = total;
+    }
+    CW_CUDA(ctx, pinned_grow(ctx->h_io, ctx->cap_h_io, total));
     int64_t nlong = 0;
     const std::vector<int32_t> order = work_order(ctx, pairs, npairs, &nlong);
-    memcpy(ctx->h_io, pairs, 8 * n);
-    memcpy(ctx->h_io + o_order, order.data(), 4 * n);
+    unsigned char* h = ctx->h_io;
+    memcpy(h, pairs, 8 * n);
+    memcpy(h + o_order, order.data(), 4 * n);
+    memset(h + o_ctr, 0, o_err + 16 - o_ctr);
+    unsigned char* d = ctx->d_call;
     cudaStream_t s = ctx->stream;
-    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_pairs1, ctx->h_io, 8 * n, cudaMemcpyHostToDevice, s));
-    CW_CUDA(ctx, cudaMemcpyAsync(ctx->d_order1, ctx->h_io + o_order, 4 * n, cudaMemcpyHostToDevice, s));
+    CW_CUDA(ctx, cudaMemcpyAsync(d, h, bytes_in, cudaMemcpyHostToDevice, s));
     cwgpu::PairArgs gl, gs;
-    split_args(ctx, ctx->d_pairs1, ctx->d_order1, npairs, nlong, ctx->d_dist1, stats_out ? ctx->d_stats1 : nullptr,
-               &gl, &gs);
-    CW_CUDA(ctx, enqueue_pairs(ctx, gl, gs, s, ctx->stream_short, ctx->ev_fork, ctx->ev_join));
-    CW_CUDA(ctx, cudaMemcpyAsync(ctx->h_io + o_dist, ctx->d_dist1, 4 * n, cudaMemcpyDeviceToHost, s));
+    split_args(ctx, reinterpret_cast<const int32_t*>(d), reinterpret_cast<const int32_t*>(d + o_order), npairs, nlong,
+               reinterpret_cast<float*>(d + o_dist),
+               stats_out ? reinterpret_cast<cwgpu_pair_stats*>(d + o_stats) : nullptr, &gl, &gs);
+    unsigned long long* ctr = reinterpret_cast<unsigned long long*>(d + o_ctr);
+    int* err = reinterpret_cast<int*>(d + o_err);
+    gl.counter = ctr;
+    gl.cells = ctr + 1;
+    gl.err = err;
+    gs.counter = ctr + 4;
+    gs.cells = ctr + 1;
+    gs.err = err;
+    CW_CUDA(ctx, enqueue_pairs(ctx, gl, gs, s, ctx->stream_short, ctx->ev_fork, ctx->ev_join, true));
+    CW_CUDA(ctx, cudaMemcpyAsync(h + o_err, d + o_err, bytes_out, cudaMemcpyDeviceToHost, s));
     if (stats_out)
-        CW_CUDA(ctx, cudaMemcpyAsync(ctx->h_io + o_stats, ctx->d_stats1, sizeof(cwgpu_pair_stats) * n,
-                                     cudaMemcpyDeviceToHost, s));
-    CW_CUDA(ctx, cudaMemcpyAsync(ctx->h_io + o_err, ctx->d_err, 4, cudaMemcpyDeviceToHost, s));
+        CW_CUDA(ctx, cudaMemcpyAsync(h + o_stats, d + o_stats, sizeof(cwgpu_pair_stats) * n, cudaMemcpyDeviceToHost, s));
     CW_CUDA(ctx, cudaStreamSynchronize(s));
-    int err = 0;
-    memcpy(&err, ctx->h_io + o_err, 4);
-    if (err) return check_kernel_error(ctx);
-    memcpy(dist_out, ctx->h_io + o_dist, 4 * n);
-    if (stats_out) memcpy(stats_out, ctx->h_io + o_stats, sizeof(cwgpu_pair_stats) * n);
+    int status = 0;
+    memcpy(&status, h + o_err, 4);
+    if (status) return status_error(ctx, status);
+    memcpy(dist_out, h + o_dist, 4 * n);
+    if (stats_out) memcpy(stats_out, h + o_stats, sizeof(cwgpu_pair_stats) * n);
     return CWGPU_OK;
 }
 

@@ -90,11 +90,8 @@ struct cwgpu_context {
     size_t cap_h_io = 0;
     // One-shot cwgpu_align_pairs: grow-only pair arrays and the second stream
     // the short-pair kernel runs on beside the long-pair one.
-    int32_t* d_pairs1 = nullptr;
-    int32_t* d_order1 = nullptr;
-    float* d_dist1 = nullptr;
-    cwgpu_pair_stats* d_stats1 = nullptr;
-    int64_t cap_pairs1 = 0;
+    unsigned char* d_call = nullptr;  // pair list, order, queue counters, status word, distances, stats
+    size_t cap_call = 0;
     cudaStream_t stream_short = nullptr;
     int prio_low = 0, prio_high = 0;  // stream priority range of the device
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
