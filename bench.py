@@ -825,9 +825,11 @@ def ours_arm(args):
         return
 
     # End to end through the C ABI with host buffers.
+    # At least --e2e-steps calls, more for short steps (about 1 s of calls, at most 100).
+    e2e_steps = max(args.e2e_steps, min(100, int(1e3 / max(ms, 1e-3))))
     e2e_times = []
     torch.cuda.set_stream(torch.cuda.default_stream())
-    for k in range(args.e2e_steps + 1):
+    for k in range(e2e_steps + 1):
         torch.cuda.synchronize()
         t = time.perf_counter()
         ctx.upload_seqs(packed=packed)
@@ -913,6 +915,7 @@ def ours_arm(args):
             "h2d_bytes_per_step": h2d,
             "d2h_bytes_per_step": d2h,
             "ms_per_step": 1e3 * e2e_s,
+            "steps": e2e_steps,
             "call": "cwgpu_upload_seqs + cwgpu_align_pairs (host pair list in, host distances out)",
         },
         "plain": {

@@ -221,7 +221,14 @@ def load(build=True):
 
 
 def _ptr(a):
-    return None if a is None else a.ctypes.data
+    """Address of a contiguous numpy array's data (None for None). A writable
+    array takes the cheaper buffer route; read-only or empty ones .ctypes."""
+    if a is None:
+        return None
+    try:
+        return ctypes.addressof(ctypes.c_char.from_buffer(a))
+    except (TypeError, ValueError, BufferError):
+        return a.ctypes.data
 
 
 def gap_penalties(params, n, m):

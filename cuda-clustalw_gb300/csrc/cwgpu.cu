@@ -611,20 +611,31 @@ int stage_inputs(cwgpu_context* ctx) {
     memcpy(h + o_lens, ctx->lens.data(), 4 * (size_t)ns);
     if (ctx->has_params) {
         int32_t* nres = reinterpret_cast<int32_t*>(h + o_nres);
-        for (int s = 0; s < ns; ++s) {
-            int c = 0;
-            const int8_t* p = ctx->host_codes.data() + ctx->offs[s];
-            for (int i = 0; i < ctx->lens[s]; ++i)
-                if (p[i] != ctx->params.gap_pos1 && p[i] != ctx->params.gap_pos2) ++c;
-            nres[s] = c;
+        const int gp1 = ctx->params.gap_pos1, gp2 = ctx->params.gap_pos2;
+        auto occurs = [&](int c) { return c >= 0 && c < CWGPU_NUMRES && ((ctx->codes_present >> c) & 1u); };
+        if (!occurs(gp1) && !occurs(gp2)) {
+            memcpy(nres, ctx->lens.data(), 4 * (size_t)ns);  // no gap codes: every position is a residue
+        } else {
+            for (int s = 0; s < ns; ++s) {
+                int c = 0;
+                const int8_t* p = ctx->host_codes.data() + ctx->offs[s];
+                for (int i = 0; i < ctx->lens[s]; ++i)
+                    if (p[i] != gp1 && p[i] != gp2) ++c;
+                nres[s] = c;
+            }
         }
-        int32_t* go = reinterpret_cast<int32_t*>(h + o_go);
-        go[0] = 0;  // L = 0 pairs never reach the penalties (:113-118)
-        for (int L = 1; L <= ctx->lmax; ++L) {
+        // Gap open by length depends only on the params: kept between calls.
+        std::vector<int32_t>& go = ctx->host_go;
+        if (go.empty() || memcmp(&ctx->go_params, &ctx->params, sizeof(cwgpu_params)) != 0) {
+            go.assign(1, 0);  // L = 0 pairs never reach the penalties (:113-118)
+            ctx->go_params = ctx->params;
+        }
+        for (int L = (int)go.size(); L <= ctx->lmax; ++L) {
             int32_t g = 0, e = 0;
             cwgpu_gap_penalties(&ctx->params, L, L, &g, &e);
-            go[L] = g;
+            go.push_back(g);
         }
+        memcpy(h + o_go, go.data(), 4 * (size_t)(ctx->lmax + 1));
     }
     if (ctx->has_matrix) {  // over the dense codes, row stride 32 (entries past K unused)
         int32_t* dm = reinterpret_cast<int32_t*>(h + o_mat);
@@ -795,26 +806,29 @@ bool short_pair(const cwgpu_context* ctx, const int32_t* pairs, int64_t q) {
 // Pairs for the long-pair kernel first, then those for the short-pair kernel
 // (*nlong of them are long); each part longest first (by n*m), so the tail of
 // each persistent queue holds its shortest work. The order only balances the
-// load, so a counting sort on a coarse key does: the top 12 bits of n*m as a
-// float (exponent and 4 mantissa bits, 1/16 relative resolution), stable.
-std::vector<int32_t> work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, int64_t* nlong) {
-    constexpr int kKeyBits = 12, kBuckets = 1 << kKeyBits;
+// load, so a stable counting sort on a coarse key does: log2(n) + log2(m) to
+// 1/16 (the sequences' len_key, kept since the upload). Writes npairs pair
+// indices to `order`.
+void work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, int32_t* order, int64_t* nlong) {
+    constexpr int kPairKeys = 2 * (cwgpu::kLenKeys - 1) + 1;  // len_key(n) + len_key(m)
+    constexpr int kBuckets = 2 * kPairKeys;                    // long pairs' keys first
     std::vector<uint16_t> key((size_t)npairs);
-    std::vector<int64_t> start(2 * kBuckets + 1, 0);
+    int64_t start[kBuckets + 1] = {0};
+    const int32_t* lens = ctx->lens.data();
+    const uint16_t* lk = ctx->len_key.data();
+    const int short_rows = ctx->short_rows;
+    int64_t nl = 0;
     for (int64_t q = 0; q < npairs; ++q) {
-        const float w = (float)((double)ctx->lens[pairs[2 * q]] * (double)ctx->lens[pairs[2 * q + 1]]);
-        uint32_t bits;
-        memcpy(&bits, &w, sizeof(bits));  // w >= 0: the bit pattern grows with w
-        const int b = (int)(bits >> (31 - kKeyBits));
-        const int k = (short_pair(ctx, pairs, q) ? kBuckets : 0) + (kBuckets - 1 - b);
+        const int a = pairs[2 * q], b = pairs[2 * q + 1];
+        const bool is_short = lens[a] <= short_rows;
+        const int k = (is_short ? kPairKeys : 0) + (kPairKeys - 1 - lk[a] - lk[b]);
         key[(size_t)q] = (uint16_t)k;
         ++start[k + 1];
+        nl += !is_short;
     }
-    for (int k = 0; k < 2 * kBuckets; ++k) start[k + 1] += start[k];
-    *nlong = start[kBuckets];
-    std::vector<int32_t> order((size_t)npairs);
-    for (int64_t q = 0; q < npairs; ++q) order[(size_t)start[key[(size_t)q]]++] = (int32_t)q;
-    return order;
+    *nlong = nl;
+    for (int k = 1; k <= kBuckets; ++k) start[k] += start[k - 1];
+    for (int64_t q = 0; q < npairs; ++q) order[start[key[(size_t)q]]++] = (int32_t)q;
 }
 
 // One persistent launch of k_pairwise<RS> over g's queue with a kernel-node
@@ -1092,14 +1106,20 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     std::vector<int64_t> doffs(nseqs);
     int64_t total = 0;
     int lmax = 0;
+    // One pass over the residues: the range check (a code outside [0, 31], read
+    // as a byte, has a bit above bit 4) and the set of codes that occur.
+    unsigned char seen[256] = {0};
     for (int s = 0; s < nseqs; ++s) {
         if (lens[s] < 0 || lens[s] > CWGPU_MAX_SEQ_LEN)
             return fail(ctx, CWGPU_ERR_ARG, "sequence length outside [0, CWGPU_MAX_SEQ_LEN]");
         if (lens[s] > 0 && (!codes || offsets[s] < 0)) return fail(ctx, CWGPU_ERR_ARG, "bad sequence offset");
+        const uint8_t* p = lens[s] > 0 ? reinterpret_cast<const uint8_t*>(codes + offsets[s]) : nullptr;
+        unsigned bits = 0;
         for (int i = 0; i < lens[s]; ++i) {
-            const int8_t c = codes[offsets[s] + i];
-            if (c < 0 || c >= CWGPU_NUMRES) return fail(ctx, CWGPU_ERR_ARG, "residue code outside [0, 31]");
+            bits |= p[i];
+            seen[p[i]] = 1;
         }
+        if (bits & ~(unsigned)(CWGPU_NUMRES - 1)) return fail(ctx, CWGPU_ERR_ARG, "residue code outside [0, 31]");
         doffs[s] = total;
         total += (lens[s] + 15) & ~15;
         lmax = std::max(lmax, (int)lens[s]);
@@ -1109,23 +1129,26 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
         if (lens[s] > 0) memcpy(packed.data() + doffs[s], codes + offsets[s], lens[s]);
     // Remap residue codes to the dense alphabet of the codes that occur, so the
     // per-stripe score profile holds K rows instead of 32.
-    bool present[CWGPU_NUMRES] = {false};
-    for (int s = 0; s < nseqs; ++s)
-        for (int i = 0; i < lens[s]; ++i) present[codes[offsets[s] + i]] = true;
     int K = 0, dense_of[CWGPU_NUMRES], code_of[CWGPU_NUMRES];
+    uint32_t codes_present = 0;
     for (int c = 0; c < CWGPU_NUMRES; ++c) {
-        dense_of[c] = present[c] ? K : -1;
-        if (present[c]) code_of[K++] = c;
+        dense_of[c] = seen[c] ? K : -1;
+        if (seen[c]) {
+            code_of[K++] = c;
+            codes_present |= 1u << c;
+        }
     }
     if (K == 0) {  // no residues at all: keep one code so launches stay well-formed
         dense_of[0] = 0;
         code_of[0] = 0;
         K = 1;
     }
+    int8_t remap[CWGPU_NUMRES];
+    for (int c = 0; c < CWGPU_NUMRES; ++c) remap[c] = (int8_t)dense_of[c];
     std::vector<int8_t> dense;
     std::vector<int64_t> poffs;
     cwgpu::build_layout(
-        nseqs, lens, [&](int s, int i) { return (int8_t)dense_of[codes[offsets[s] + i]]; }, dense, poffs);
+        nseqs, lens, [&](int s) { return lens[s] > 0 ? codes + offsets[s] : nullptr; }, remap, dense, poffs);
     // The device copy is made by the next call that needs it (stage_inputs),
     // in one copy together with the tables derived from params and matrix.
     ctx->host_layout.swap(dense);
@@ -1133,8 +1156,11 @@ int cwgpu_upload_seqs(cwgpu_context* ctx, int32_t nseqs, const int8_t* codes, co
     ctx->nseqs = nseqs;
     ctx->lmax = lmax;
     ctx->lens.assign(lens, lens + nseqs);
-    ctx->offs = doffs;
+    ctx->len_key.resize((size_t)nseqs);
+    for (int s = 0; s < nseqs; ++s) ctx->len_key[(size_t)s] = (uint16_t)cwgpu::len_key(lens[s]);
+    ctx->offs.swap(doffs);
     ctx->host_codes.swap(packed);
+    ctx->codes_present = codes_present;
     ctx->K = K;
     memcpy(ctx->dense_of, dense_of, sizeof(dense_of));
     memcpy(ctx->code_of, code_of, sizeof(code_of));
@@ -1163,7 +1189,8 @@ int cwgpu_plan_create(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
     if (e == cudaSuccess) e = cudaMalloc(&p->d_dist, sizeof(float) * np);
     if (e == cudaSuccess) e = cudaMalloc(&p->d_stats, sizeof(cwgpu_pair_stats) * np);
     if (e == cudaSuccess && npairs > 0) {
-        std::vector<int32_t> order = work_order(ctx, pairs, npairs, &p->nlong);
+        std::vector<int32_t> order((size_t)npairs);
+        work_order(ctx, pairs, npairs, order.data(), &p->nlong);
         e = cudaMemcpy(p->d_pairs, pairs, sizeof(int32_t) * 2 * npairs, cudaMemcpyHostToDevice);
         if (e == cudaSuccess) e = cudaMemcpy(p->d_order, order.data(), sizeof(int32_t) * npairs, cudaMemcpyHostToDevice);
     }
@@ -1289,10 +1316,9 @@ int cwgpu_align_pairs(cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, 
     }
     CW_CUDA(ctx, pinned_grow(ctx->h_io, ctx->cap_h_io, total));
     int64_t nlong = 0;
-    const std::vector<int32_t> order = work_order(ctx, pairs, npairs, &nlong);
     unsigned char* h = ctx->h_io;
+    work_order(ctx, pairs, npairs, reinterpret_cast<int32_t*>(h + o_order), &nlong);
     memcpy(h, pairs, 8 * n);
-    memcpy(h + o_order, order.data(), 4 * n);
     memset(h + o_ctr, 0, o_err + 16 - o_ctr);
     unsigned char* d = ctx->d_call;
     cudaStream_t s = ctx->stream;

@@ -32,6 +32,18 @@ cudaError_t cwgpu_enqueue_pair_kernels(const cwgpu::PairArgs& gl, const cwgpu::P
                                        int grid_short, int prio_high, int prio_low, cudaStream_t s, cudaStream_t s2,
                                        cudaEvent_t fork, cudaEvent_t join);
 
+namespace cwgpu {
+// Sort key of a sequence length: 16 * floor(log2 L) plus the 4 bits below the
+// leading one (log2 L to 1/16), 0 for L = 0; below kLenKeys for L <= 65535.
+constexpr int kLenKeys = 16 * 16;
+inline int len_key(int L) {
+    if (L <= 0) return 0;
+    const int e = 31 - __builtin_clz((unsigned)L);
+    const int m = e >= 4 ? (L >> (e - 4)) & 15 : (L << (4 - e)) & 15;
+    return 16 * e + m;
+}
+}  // namespace cwgpu
+
 struct cwgpu_context {
     int device = 0;
     int sm_count = 0;
@@ -42,8 +54,10 @@ struct cwgpu_context {
     int nseqs = 0;
     int lmax = 0;
     std::vector<int32_t> lens;
+    std::vector<uint16_t> len_key;  // cwgpu::len_key of each length (the work order's key)
     std::vector<int64_t> offs;
     std::vector<int8_t> host_codes;  // original codes, for nres and the remap
+    uint32_t codes_present = 0;      // bit c: code c occurs in some sequence
     int K = 0;                       // codes present in the sequences
     int dense_of[CWGPU_NUMRES];      // original code -> dense index, -1 if absent
     int code_of[CWGPU_NUMRES];       // dense index -> original code
@@ -66,6 +80,8 @@ struct cwgpu_context {
     bool in_dirty = true;
     std::vector<int8_t> host_layout;  // d_codes as built on the host
     std::vector<int64_t> host_poffs;
+    std::vector<int32_t> host_go;     // gap open by length 0..: valid for go_params
+    cwgpu_params go_params;
     int8_t* d_codes = nullptr;   // pair kernels' layout (cwgpu_layout.h): guards, forward and reversed copies
     int64_t* d_poffs = nullptr;  // forward copy of each sequence in d_codes
     int64_t* d_offs = nullptr;   // each sequence in host_codes (the quick path's upload of it)

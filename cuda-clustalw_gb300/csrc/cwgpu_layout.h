@@ -25,10 +25,13 @@ constexpr int kGuard = 64;
 
 __host__ __device__ inline long long rev_offset(int len) { return ((long long)len + 15) & ~15LL; }
 
-// Lays out n sequences; code_at(s, i) gives residue i of sequence s. Fills
-// `out` (the whole buffer) and `offs` (offset of each forward copy).
-template <class CodeAt>
-void build_layout(int n, const int32_t* lens, CodeAt code_at, std::vector<int8_t>& out, std::vector<int64_t>& offs) {
+// Lays out n sequences: sequence s is the lens[s] codes at row(s), each code c
+// (in [0, 31]) stored as remap[c]. Fills `out` (the whole buffer) and `offs`
+// (offset of each forward copy). The remap table is copied to a local array
+// so that the byte stores of the layout cannot alias it.
+template <class Row>
+void build_layout(int n, const int32_t* lens, Row row, const int8_t* remap, std::vector<int8_t>& out,
+                  std::vector<int64_t>& offs) {
     offs.resize((size_t)n);
     int64_t total = kGuard;
     for (int s = 0; s < n; ++s) {
@@ -37,14 +40,17 @@ void build_layout(int n, const int32_t* lens, CodeAt code_at, std::vector<int8_t
     }
     total += kGuard;
     out.assign((size_t)total, 0);
+    int8_t map[32];
+    memcpy(map, remap, sizeof(map));
     for (int s = 0; s < n; ++s) {
+        const int8_t* src = row(s);
         int8_t* f = out.data() + offs[(size_t)s];
-        int8_t* r = f + rev_offset(lens[s]);
         const int L = lens[s];
+        int8_t* r = f + rev_offset(L) + (L - 1);
         for (int i = 0; i < L; ++i) {
-            const int8_t c = code_at(s, i);
+            const int8_t c = map[src[i] & 31];
             f[i] = c;
-            r[L - 1 - i] = c;
+            r[-i] = c;
         }
     }
 }

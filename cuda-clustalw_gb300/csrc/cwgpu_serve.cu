@@ -231,9 +231,11 @@ void remap_job(cwgpu_server* s, Job* j, const int8_t* codes, const int64_t* offs
                 s->matrix_dirty = true;
             }
         }
+    int8_t remap[CWGPU_NUMRES];
+    for (int c = 0; c < CWGPU_NUMRES; ++c) remap[c] = (int8_t)s->dense_of[c];
     cwgpu::build_layout(
-        j->nseqs, j->lens.data(), [&](int q, int i) { return (int8_t)s->dense_of[codes[offsets[q] + i]]; }, j->codes,
-        j->offs);
+        j->nseqs, j->lens.data(), [&](int q) { return j->lens[q] > 0 ? codes + offsets[q] : nullptr; }, remap,
+        j->codes, j->offs);
     j->nres.resize(j->nseqs);
     for (int q = 0; q < j->nseqs; ++q) {
         int r = 0;
