@@ -51,6 +51,7 @@ for _p in (REPO, os.path.join(REPO, "cuda-clustalw_gb300")):
 FP64_NOMINAL_TFLOPS = 1.25  # GB300 nominal dense fp64 (an FMA counts 2; the join's criterion has none)
 OPS_PER_CELL = 8  # E, F via __viaddmax (2), H-gap term (1), diag add + 3-way max (2), max tracking (2), score (1)
 INT32_LANES_PER_SM = 128
+ALU_PIPE_LANES_PER_SM = 64  # integer ALU pipe (IMNMX, IADD3, DPX): half the INT32 lane rate
 
 WORKLOADS = {
     # name: (kind, generator args)
@@ -883,6 +884,12 @@ def ours_arm(args):
         # DRAM bytes per launch over the launch time: how far the kernel is from the HBM roof
         "hbm_achieved_gbs": (tpc * cells_nm / (ms / 1e3) / 1e9) if tpc is not None else None,
         "traffic_source": tsrc,
+        # The recurrence's max, add and DPX instructions all issue on the
+        # integer ALU pipe, which takes half the INT32 lane rate (64 lanes per
+        # SM per clock): the same operation count against that pipe's rate.
+        "alu_pipe": {"peak": peak_tops * ALU_PIPE_LANES_PER_SM / INT32_LANES_PER_SM,
+                     "frac": achieved / (peak_tops * ALU_PIPE_LANES_PER_SM / INT32_LANES_PER_SM),
+                     "lanes_per_sm": ALU_PIPE_LANES_PER_SM},
     }
 
     line = {
