@@ -15,7 +15,7 @@ LIB_DIR = os.path.join(PKG_ROOT, "lib")
 LIB_PATH = os.path.join(LIB_DIR, "libcwgpu.so")
 
 SOURCES = ["cwgpu.cu", "cwgpu_noalloc.cu", "cwgpu_serve.cu", "cwgpu_nj.cu", "cwgpu_fast.cu"]
-HEADERS = ["cwgpu_device.cuh", "cwgpu_context.h", "cwgpu_ranges.h", "cwgpu_layout.h"]
+HEADERS = ["cwgpu_device.cuh", "cwgpu_context.h", "cwgpu_ranges.h", "cwgpu_layout.h", "cwgpu_order.h"]
 ARCH_FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

@@ -803,32 +803,9 @@ bool short_pair(const cwgpu_context* ctx, const int32_t* pairs, int64_t q) {
     return ctx->lens[pairs[2 * q]] <= ctx->short_rows;
 }
 
-// Pairs for the long-pair kernel first, then those for the short-pair kernel
-// (*nlong of them are long); each part longest first (by n*m), so the tail of
-// each persistent queue holds its shortest work. The order only balances the
-// load, so a stable counting sort on a coarse key does: log2(n) + log2(m) to
-// 1/16 (the sequences' len_key, kept since the upload). Writes npairs pair
-// indices to `order`.
+// The order the persistent kernels take the pairs in (cwgpu_order.h).
 void work_order(const cwgpu_context* ctx, const int32_t* pairs, int64_t npairs, int32_t* order, int64_t* nlong) {
-    constexpr int kPairKeys = 2 * (cwgpu::kLenKeys - 1) + 1;  // len_key(n) + len_key(m)
-    constexpr int kBuckets = 2 * kPairKeys;                    // long pairs' keys first
-    std::vector<uint16_t> key((size_t)npairs);
-    int64_t start[kBuckets + 1] = {0};
-    const int32_t* lens = ctx->lens.data();
-    const uint16_t* lk = ctx->len_key.data();
-    const int short_rows = ctx->short_rows;
-    int64_t nl = 0;
-    for (int64_t q = 0; q < npairs; ++q) {
-        const int a = pairs[2 * q], b = pairs[2 * q + 1];
-        const bool is_short = lens[a] <= short_rows;
-        const int k = (is_short ? kPairKeys : 0) + (kPairKeys - 1 - lk[a] - lk[b]);
-        key[(size_t)q] = (uint16_t)k;
-        ++start[k + 1];
-        nl += !is_short;
-    }
-    *nlong = nl;
-    for (int k = 1; k <= kBuckets; ++k) start[k] += start[k - 1];
-    for (int64_t q = 0; q < npairs; ++q) order[start[key[(size_t)q]]++] = (int32_t)q;
+    cwgpu::work_order(ctx->lens.data(), ctx->len_key.data(), ctx->short_rows, pairs, npairs, order, nlong);
 }
 
 // One persistent launch of k_pairwise<RS> over g's queue with a kernel-node

@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "cwgpu.h"
+#include "cwgpu_order.h"
 
 struct cwgpu_fast_state;
 // Frees the quick-distance tables of a context (cwgpu_fast.cu).
@@ -31,18 +32,6 @@ int cwgpu_pair_kernel_warps_per_cta();
 cudaError_t cwgpu_enqueue_pair_kernels(const cwgpu::PairArgs& gl, const cwgpu::PairArgs& gs, int grid,
                                        int grid_short, int prio_high, int prio_low, cudaStream_t s, cudaStream_t s2,
                                        cudaEvent_t fork, cudaEvent_t join);
-
-namespace cwgpu {
-// Sort key of a sequence length: 16 * floor(log2 L) plus the 4 bits below the
-// leading one (log2 L to 1/16), 0 for L = 0; below kLenKeys for L <= 65535.
-constexpr int kLenKeys = 16 * 16;
-inline int len_key(int L) {
-    if (L <= 0) return 0;
-    const int e = 31 - __builtin_clz((unsigned)L);
-    const int m = e >= 4 ? (L >> (e - 4)) & 15 : (L << (4 - e)) & 15;
-    return 16 * e + m;
-}
-}  // namespace cwgpu
 
 struct cwgpu_context {
     int device = 0;
