@@ -15,7 +15,7 @@
 // address; a kernel given it would fault or read the wrong memory. So the
 // first call on each device, with that device current, looks the address up
 // with cudaGetSymbolAddress (and the occupancy of the kernel) and caches both
-// per device. That first call should come before any stream capture.
+// per device.
 //
 // All calls share the one array and keep the last call's contents; the
 // control words are cleared at the start of each call. Calls whose GPU work

@@ -189,8 +189,8 @@ void cwgpu_plan_destroy(cwgpu_plan* plan);
  * memory: codes/offsets/lens as for cwgpu_upload_seqs, d_matrix the 32x32
  * int32 matrix, d_pairs 2*npairs int32, outputs d_dist (npairs floats) and
  * d_stats (nullable). The first call on a device looks up the array's device
- * address and should come before any stream capture. The call waits for its
- * kernel on `stream` (a cudaStream_t, NULL = legacy default) and returns
+ * address. The call waits for its kernel on `stream` (a cudaStream_t, NULL =
+ * legacy default) and returns
  * CWGPU_ERR_ARG if the device-side checks rejected an input (pair index,
  * negative sequence offset, length above max_len, residue code outside
  * [0, 31]), CWGPU_ERR_MATRIX if a d_matrix entry is outside int16 (nothing is
