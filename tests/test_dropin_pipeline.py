@@ -68,7 +68,7 @@ def programs():
     with ThreadPoolExecutor(max_workers=os.cpu_count() or 4) as ex:
         list(ex.map(compile_one, jobs))
     stub = os.path.join(d, "stub.o")
-    subprocess.run(["gcc", "-O2", "-c", "-I" + os.path.join(REPO, "include"),
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-c", "-I" + os.path.join(REPO, "include"),
                     os.path.join(REPO, "tests", "dropin_stub_cwgpu.c"), "-o", stub], check=True)
     common = [o for _, o in jobs[:len(units)]]
     ref_bin, bound_bin = os.path.join(d, "clustalw2"), os.path.join(d, "clustalw2_dropin")

@@ -30,7 +30,7 @@ def runner(tmp_path_factory, oracle_mod):
         pytest.skip("oracle/build_ref.sh did not build the reference objects")
     d = tmp_path_factory.mktemp("dropin_run")
     stub = str(d / "stub.o")
-    subprocess.run(["gcc", "-O2", "-c", "-I" + os.path.join(REPO, "include"),
+    subprocess.run(["gcc", "-O2", "-ffp-contract=off", "-c", "-I" + os.path.join(REPO, "include"),
                     os.path.join(REPO, "tests", "dropin_stub_cwgpu.c"), "-o", stub], check=True)
     host = os.path.join(REPO, "cuda-clustalw_gb300", "host")
     out = str(d / "dropin_run")
