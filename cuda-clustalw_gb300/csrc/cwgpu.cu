@@ -90,10 +90,12 @@ __global__ void __launch_bounds__(kWarpsPerBlock * 32, 5)
 // warp per pair leaves most of the GPU idle. Here a CTA of nw warps aligns one
 // pair: forwardPass and reversePass are shared sweeps (cwgpu::sweep_mw) over
 // all nw warps, whose results are reduced across the warps; Myers-Miller
-// frames of at least large_rows rows are divided by the two halves of the CTA
-// at once (forward half on warps [0, nw/2), reverse half on [nw/2, nw)), and
-// the smaller frames they leave go to a shared stack that every warp takes
-// frames from (cwgpu::mm_align) and gives the children it makes back to. Frames are independent once (A, B, M, N, tb, te) are
+// frames of at least large_rows rows (0: the larger of 512 and a third of the
+// pair's diff() box) are divided by the two halves of the CTA at once (forward
+// half on warps [0, nw/2), reverse half on [nw/2, nw)), or two such frames at
+// once on half the CTA each, and the smaller frames they leave go to a shared
+// stack that every warp takes frames from (cwgpu::mm_align) and gives the
+// children it makes back to. Frames are independent once (A, B, M, N, tb, te) are
 // known and diff()'s identity and match counts are sums over its M == 1
 // leaves, so results equal those of the one-warp form.
 constexpr int kCtaMaxWarps = 16;
@@ -237,17 +239,20 @@ __device__ void cta_diff(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, 
                          const cwgpu::Env& X, cwgpu::MwSync& mw, unsigned long long& epoch, const CtaArgs& ca,
                          int& mm_score, int& n_ident, int& n_match, long long& cells) {
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int half = nw / 2;
     int2* bufA = bufs + (size_t)warp * stride;
     int2* bufB = bufA + stride / 2;
     int ident = 0, match = 0;
     long long ncell = 0;
+    // Frames divided by the CTA: at least large_rows rows; automatically the
+    // top two levels of the recursion (measured on one-column calls of 1523
+    // residues and sets of 3000: both faster than a fixed 512 or 1024).
+    const int large_rows = ca.large_rows > 0 ? ca.large_rows : max(512, M0 / 3);
     if (threadIdx.x == 0) {
         C.nstack = 0;
         C.nsmall = 0;
         C.mm = 0;
         const int4 root = make_int4(A0, B0, M0 | kRootBit, N0);
-        if (cta_large(M0, N0, ca.large_rows))
+        if (cta_large(M0, N0, large_rows))
             C.stack[C.nstack++] = root;
         else
             C.small[C.nsmall++] = root;
@@ -256,15 +261,25 @@ __device__ void cta_diff(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, 
     for (;;) {
         const int ns = C.nstack;
         if (ns == 0) break;
-        const int4 F = C.stack[ns - 1];
-        __syncthreads();  // every thread has the frame before it is popped
-        if (threadIdx.x == 0) C.nstack = ns - 1;
+        // One large frame by the whole CTA, or, when two are waiting, both at
+        // once: frame f on warps [f * nw / 2, (f + 1) * nw / 2), forward half
+        // on the first half of those warps, reverse half on the second.
+        const int k = (ns >= 2 && nw >= 4) ? 2 : 1;
+        const int gw = nw / (2 * k);  // warps per half
+        const int fi = warp / (2 * gw);
+        const int4 F = C.stack[ns - 1 - fi];
+        int4 Fs[2];
+        Fs[0] = C.stack[ns - 1];
+        Fs[1] = k > 1 ? C.stack[ns - 2] : Fs[0];
+        __syncthreads();  // every thread has its frames before they are popped
+        if (threadIdx.x == 0) C.nstack = ns - k;
         const int A = F.x, B = F.y, M = F.z & ~kRootBit;
         const int N = F.w & ((1 << 29) - 1);
         const int tbf = (F.w >> 29) & 1, tef = (F.w >> 30) & 1;
         const int tb = tbf ? go : 0, te = tef ? go : 0;
         const int midi = M / 2;
-        const bool fwd_group = warp < half;
+        const bool fwd_group = warp - fi * 2 * gw < gw;
+        const int slot0 = fi * 2 * gw + (fwd_group ? 0 : gw);
         cwgpu::Task t;
         if (fwd_group) {
             t.rseq = s1 + A;
@@ -285,36 +300,44 @@ __device__ void cta_diff(CtaCtl& C, const int8_t* s1, const int8_t* s1r, int n, 
         t.fo = go;
         mw.epoch = (++epoch) << 32;
         cwgpu::Best unused;
-        cwgpu::sweep_mw<RS, cwgpu::MODE_GLOBAL>(t, go, ge, 0, X, unused, bufs, stride, fwd_group ? 0 : half,
-                                                fwd_group ? warp : warp - half, half, mw, &C.stop);
+        cwgpu::sweep_mw<RS, cwgpu::MODE_GLOBAL>(t, go, ge, 0, X, unused, bufs, stride, slot0, warp - slot0, gw, mw,
+                                                &C.stop);
         __syncthreads();
         if (warp == 0) {
-            ncell += (long long)M * N;
-            const int2* fwd = bufs + (size_t)cwgpu::mw_last_rank(midi, RS, half) * stride;
-            const int2* rev = bufs + (size_t)(half + cwgpu::mw_last_rank(M - midi, RS, half)) * stride;
-            int midh, midj;
-            bool type2;
-            cwgpu::midpoint_scan(fwd, rev, M, N, midi, tb, te, go, ge, midh, midj, type2);
-            if (lane == 0) {
-                if (F.z & kRootBit) C.mm = midh;
-                int4 ch[2];  // right, then left, as diff() pushes them (:598-609)
-                if (!type2) {
-                    ch[0] = make_int4(A + midi, B + midj, M - midi, (N - midj) | (1 << 29) | (tef << 30));
-                    ch[1] = make_int4(A, B, midi, midj | (tbf << 29) | (1 << 30));
-                } else {
-                    ch[0] = make_int4(A + midi + 1, B + midj, M - midi - 1, (N - midj) | (tef << 30));
-                    ch[1] = make_int4(A, B, midi - 1, midj | (tbf << 29));
+            for (int f = 0; f < k; ++f) {
+                const int4 G = Fs[f];
+                const int GA = G.x, GB = G.y, GM = G.z & ~kRootBit;
+                const int GN = G.w & ((1 << 29) - 1);
+                const int gtbf = (G.w >> 29) & 1, gtef = (G.w >> 30) & 1;
+                const int gmidi = GM / 2;
+                ncell += (long long)GM * GN;
+                const int2* fwd = bufs + (size_t)(f * 2 * gw + cwgpu::mw_last_rank(gmidi, RS, gw)) * stride;
+                const int2* rev = bufs + (size_t)(f * 2 * gw + gw + cwgpu::mw_last_rank(GM - gmidi, RS, gw)) * stride;
+                int midh, midj;
+                bool type2;
+                cwgpu::midpoint_scan(fwd, rev, GM, GN, gmidi, gtbf ? go : 0, gtef ? go : 0, go, ge, midh, midj, type2);
+                if (lane == 0) {
+                    if (G.z & kRootBit) C.mm = midh;
+                    int4 ch[2];  // right, then left, as diff() pushes them (:598-609)
+                    if (!type2) {
+                        ch[0] = make_int4(GA + gmidi, GB + midj, GM - gmidi, (GN - midj) | (1 << 29) | (gtef << 30));
+                        ch[1] = make_int4(GA, GB, gmidi, midj | (gtbf << 29) | (1 << 30));
+                    } else {
+                        ch[0] = make_int4(GA + gmidi + 1, GB + midj, GM - gmidi - 1, (GN - midj) | (gtef << 30));
+                        ch[1] = make_int4(GA, GB, gmidi - 1, midj | (gtbf << 29));
+                    }
+                    for (int c = 0; c < 2; ++c) {
+                        if (cta_large(ch[c].z, ch[c].w & ((1 << 29) - 1), large_rows) && C.nstack < kCtaStack)
+                            C.stack[C.nstack++] = ch[c];
+                        else
+                            C.small[C.nsmall++] = ch[c];
+                    }
                 }
-                for (int c = 0; c < 2; ++c) {
-                    if (cta_large(ch[c].z, ch[c].w & ((1 << 29) - 1), ca.large_rows) && C.nstack < kCtaStack)
-                        C.stack[C.nstack++] = ch[c];
-                    else
-                        C.small[C.nsmall++] = ch[c];
-                }
+                __syncwarp();
             }
         }
         __syncthreads();
-        if (C.nsmall > kCtaSmall - 2)
+        if (C.nsmall > kCtaSmall - 4)
             cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ca, ident, match, ncell);
     }
     cta_small_frames<RS>(C, s1, s1r, n, s2, s2r, m, go, ge, bufA, bufB, X, ca, ident, match, ncell);
@@ -1408,10 +1431,10 @@ int cwgpu_set_tuning(cwgpu_context* ctx, const cwgpu_tuning* tuning) {
 int cwgpu_set_cta_tuning(cwgpu_context* ctx, const cwgpu_cta_tuning* t) {
     if (!ctx || !t) return CWGPU_ERR_ARG;
     const int w = t->warps;
-    if (t->max_pairs < -1 || !(w == 0 || w == 2 || w == 4 || w == 8 || w == 16) || t->large_rows < 2 ||
-        t->large_rows > CWGPU_MAX_SEQ_LEN)
+    if (t->max_pairs < -1 || !(w == 0 || w == 2 || w == 4 || w == 8 || w == 16) ||
+        (t->large_rows != 0 && t->large_rows < 2) || t->large_rows > CWGPU_MAX_SEQ_LEN)
         return fail(ctx, CWGPU_ERR_ARG,
-                    "max_pairs must be >= -1, warps 0, 2, 4, 8 or 16, large_rows in [2, 65535]");
+                    "max_pairs must be >= -1, warps 0, 2, 4, 8 or 16, large_rows 0 or in [2, 65535]");
     ctx->cta_pairs = t->max_pairs;
     ctx->cta_warps = w;
     ctx->cta_large_rows = t->large_rows;

@@ -55,8 +55,9 @@ struct cwgpu_context {
     // One CTA per pair (k_pairwise_cta) for launches of at most cta_pairs long
     // pairs (-1: a quarter of the long-pair kernel's warps): cta_warps warps
     // per CTA (0: chosen by pairs per SM), Myers-Miller frames of at least
-    // cta_large_rows rows divided by the whole CTA.
-    int cta_pairs = -1, cta_warps = 0, cta_large_rows = 1024;
+    // cta_large_rows rows divided by the whole CTA (0: per pair, the larger of
+    // 512 and a third of its diff() box).
+    int cta_pairs = -1, cta_warps = 0, cta_large_rows = 0;
     int grid_cta[5] = {0, 0, 0, 0, 0};  // CTAs of k_pairwise_cta that fit at once, by log2(warps), for grid_K
     // Inputs on the device: one arena, filled by one copy from one pinned
     // staging buffer whenever the host-side inputs changed (cwgpu_stage_inputs).

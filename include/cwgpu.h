@@ -224,11 +224,14 @@ int cwgpu_get_tuning(const cwgpu_context* ctx, cwgpu_tuning* tuning);
  * short_rows) runs them one CTA of `warps` warps (2, 4, 8 or 16) per pair
  * instead of one warp per pair: the warps share the pair's forwardPass and
  * reversePass stripes and every Myers-Miller frame of at least large_rows
- * rows; smaller frames go to a stack in shared memory from which the warps
- * take frames and to which they give back the children they make. Defaults: max_pairs -1 (a
- * quarter of the long-pair kernel's resident warps, 760 on a GB300), warps 0
- * (16, 8 or 4 as the launch has at most 0.5, 2.5 or more pairs per SM),
- * large_rows 1024; max_pairs 0 turns it off. The reference's own GPU form also
+ * rows (two such frames at once on half the CTA each when two are waiting);
+ * smaller frames go to a stack in shared memory from which the warps take
+ * frames and to which they give back the children they make. Defaults:
+ * max_pairs -1 (a quarter of the long-pair kernel's resident warps, 760 on a
+ * GB300), warps 0 (16, 8 or 4 as the launch has at most 0.5, 2.5 or more pairs
+ * per SM), large_rows 0 (per pair, the larger of 512 and a third of the rows
+ * of its diff() box: the top two levels of the recursion); max_pairs 0 turns
+ * it off. The reference's own GPU form also
  * runs one CTA per pair (G/cuda/cudaFullPairwiseAlign.cu:369-468), as one
  * 32-thread wavefront. A hand-over wait between the warps that ran out its
  * bound ends the call with CWGPU_ERR_TIMEOUT. */

@@ -65,11 +65,13 @@ def test_cta_form_bit_exact(ctx, oracle_mod, name):
         ctx.set_cta_tuning(*old)
 
 
-@pytest.mark.parametrize("warps,large_rows", [(2, 768), (4, 256), (8, 2), (8, 65535), (16, 512), (16, 768)])
+@pytest.mark.parametrize("warps,large_rows", [(2, 768), (4, 256), (8, 2), (8, 65535), (16, 512), (16, 768), (8, 0),
+                                             (16, 0), (4, 0)])
 def test_cta_form_knobs_keep_results(ctx, oracle_mod, warps, large_rows):
     """Warps per CTA and the size from which the CTA divides a frame together
     change only the schedule (large_rows 2: every frame with 64 columns or
-    more; 65535: none, every frame to one warp)."""
+    more, two at a time whenever two are waiting; 65535: none, every frame to
+    one warp; 0: the automatic threshold)."""
     g = load_golden("synth_long_6x3000")
     setup(ctx, g)
     old = ctx.get_cta_tuning()
@@ -108,7 +110,7 @@ def test_one_column_call_takes_the_cta_form_by_default(ctx):
     n = len(g["seqs"])
     pairs = range_pairs(n, 0, n, n - 2, n)
     assert len(pairs) == n - 1
-    assert ctx.get_cta_tuning() == (-1, 0, 1024)  # defaults: automatic threshold and warps
+    assert ctx.get_cta_tuning() == (-1, 0, 0)  # defaults: automatic threshold, warps and frame size
     plan = ctx.plan(pairs)
     assert plan.pair_ctas()
     plan.close()
